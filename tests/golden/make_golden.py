@@ -1,0 +1,159 @@
+"""Generate golden input/output vectors from the reference implementation itself.
+
+Run in a container that has the reference source checked out (default ``/root/reference``,
+override with ``WALRUS_REFERENCE``).  numba is not needed: a stub module turns ``numba.jit``
+into the identity and ``numba.prange`` into ``range``, so the reference's own Python code runs
+as plain NumPy.  The package ``__init__`` (which pulls in dask) is bypassed by registering a bare
+``thewalrus`` package whose path is the reference's source directory.
+
+One reference quirk is guarded: ``charpoly.powertrace`` of a 0x0 matrix indexes an empty array
+(thewalrus/charpoly.py:215-217); the guard returns the values the reference's loops produce
+around that read (p_0 = 0 followed by zeros).
+
+Output: ``reference_cases.npz`` next to this script.  Keys are ``<family>/<index>/<field>``.
+"""
+import os
+import sys
+import time
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from thewalrus_gb300 import workloads as wl  # noqa: E402
+
+
+def import_reference(path):
+    stub = types.ModuleType("numba")
+
+    def jit(*args, **kwargs):
+        if args and callable(args[0]) and not kwargs:
+            return args[0]
+        return lambda f: f
+
+    stub.jit = jit
+    stub.njit = jit
+    stub.prange = range
+    sys.modules["numba"] = stub
+    pkg = types.ModuleType("thewalrus")
+    pkg.__path__ = [os.path.join(path, "thewalrus")]
+    sys.modules["thewalrus"] = pkg
+    import thewalrus.charpoly as cp
+    import thewalrus._hafnian as hf
+    import thewalrus.loop_hafnian_batch as lb
+    import thewalrus.reference as ref
+
+    orig = cp.powertrace
+
+    def guarded(H, n):
+        if len(H) == 0:
+            return np.zeros(n + 2, dtype=H.dtype)
+        return orig(H, n)
+
+    cp.powertrace = guarded
+    return cp, hf, lb, ref
+
+
+def main():
+    path = os.environ.get("WALRUS_REFERENCE", "/root/reference")
+    cp, hf, lb, ref = import_reference(path)
+    rng = np.random.default_rng(20261203)
+    out = {}
+    counts = {}
+
+    def put(family, **fields):
+        i = counts.get(family, 0)
+        counts[family] = i + 1
+        for k, v in fields.items():
+            out["%s/%d/%s" % (family, i, k)] = np.asarray(v)
+
+    t0 = time.time()
+    # plain hafnian through the public API (method="glynn")
+    for n in (6, 8, 10, 12, 14, 16, 18, 20):
+        A = wl.complex_symmetric(n, seed=100 + n)
+        put("haf", A=A, out=hf.hafnian(A))
+    for n in (6, 10, 14, 16):
+        A = wl.real_signed(n, seed=200 + n)
+        put("haf", A=A, out=hf.hafnian(A))
+    for n in (8, 12, 16):
+        A = wl.real_nonneg(n, seed=300 + n)
+        put("haf", A=A, out=hf.hafnian(A))
+    for n in (10, 16):
+        A = wl.adjacency01(n, seed=400 + n)
+        put("haf", A=A, out=hf.hafnian(A))
+    A = np.ones((12, 12), dtype=np.int64)
+    put("haf", A=A, out=hf.hafnian(A))
+    # the 24x24 plain-hafnian workload (seed 0) and the all-ones 24x24 matrix
+    A = wl.complex_symmetric(24, seed=0)
+    put("haf", A=A, out=hf.hafnian(A))
+    A = np.ones((24, 24))
+    put("haf", A=A, out=hf.hafnian(A))
+    # inclusion/exclusion variant
+    for n in (8, 12):
+        A = wl.complex_symmetric(n, seed=500 + n)
+        put("haf_inclexcl", A=A, out=hf.hafnian(A, method="inclexcl"))
+
+    # loop hafnian through the public API
+    for n in (5, 6, 7, 8, 9, 11, 12, 15, 16):
+        A = wl.complex_symmetric(n, seed=600 + n)
+        put("lhaf", A=A, out=hf.hafnian(A, loop=True))
+    for n in (6, 9, 14):
+        A = wl.real_signed(n, seed=700 + n)
+        put("lhaf", A=A, out=hf.hafnian(A, loop=True))
+
+    # hafnian_repeated, plain and loop, random repetitions 0..3
+    for case in range(14):
+        n = int(rng.integers(2, 8))
+        A = wl.complex_symmetric(n, seed=800 + case)
+        rpt = rng.integers(0, 4, size=n)
+        if rpt.sum() == 0:
+            rpt[0] = 2
+        mu = (rng.normal(size=n) + 1j * rng.normal(size=n)) * 0.5
+        if rpt.sum() % 2 == 0:
+            put("rep", A=A, rpt=rpt, out=hf.hafnian_repeated(A, list(rpt)))
+        put("rep_loop", A=A, rpt=rpt, mu=mu,
+            out=hf.hafnian_repeated(A, list(rpt), mu=mu, loop=True))
+    # repeated edges that produce all-zero deltas (0x0 term matrices)
+    A = np.array([[1.0]])
+    put("rep", A=A, rpt=np.array([12]), out=hf.hafnian_repeated(A, [12]))
+    A = np.array([[0.0, 1.0], [1.0, 0.0]], dtype=np.complex128)
+    put("rep", A=A, rpt=np.array([6, 6]), out=hf.hafnian_repeated(A, [6, 6]))
+
+    # the loop-hafnian Gaussian-state workload at reduced size: 6 modes, 12 photons
+    A, gamma, rpt = wl.gaussian_state_loop(modes=6, seed=1, photons=12, max_rep=3)
+    put("rep_loop", A=A, rpt=rpt, mu=gamma,
+        out=hf.hafnian_repeated(A, list(rpt), mu=gamma, loop=True))
+
+    # loop_hafnian_batch: even and odd pairing paths
+    for case in range(8):
+        modes = int(rng.integers(3, 7))
+        calls = wl.batch_loop_calls(count=1, seed=900 + case, modes=modes,
+                                    cutoff=int(rng.integers(2, 7)), max_fixed=2)
+        B, D, fixed, cutoff = calls[0]
+        put("batch", A=B, D=D, fixed=fixed, cutoff=cutoff,
+            out=lb.loop_hafnian_batch(B, D, fixed, cutoff))
+
+    # brute-force matchings from thewalrus/reference.py for small n
+    for n in (4, 6, 8):
+        A = wl.complex_symmetric(n, seed=1000 + n)
+        put("brute", A=A, loop=False, out=ref.hafnian(A))
+    for n in (3, 5, 7):
+        A = wl.complex_symmetric(n, seed=1100 + n)
+        put("brute", A=A, loop=True, out=ref.hafnian(A, loop=True))
+
+    # charpoly.powertrace: matmul branch (n <= m) and La Budde branch (n > m)
+    for m, n in ((4, 3), (4, 7), (6, 4), (6, 9), (8, 12)):
+        H = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+        put("ptrace", H=H, n=n, out=cp.powertrace(H.copy(), n))
+    for m in (2, 5, 9):
+        H = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
+        put("charpoly", H=H, out=np.array(cp.charpoly(H.copy())))
+
+    np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
+    print("wrote %d arrays for %s in %.1fs" % (len(out), counts, time.time() - t0))
+
+
+if __name__ == "__main__":
+    main()
