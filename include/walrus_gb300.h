@@ -1,0 +1,108 @@
+/*
+ * walrus_gb300: C ABI of the GB300 (sm_103a) hafnian / loop-hafnian finite-difference sieve.
+ *
+ * The host side (input validation, special cases, edge pairing, reordering) stays in the
+ * caller; these entry points replace the reference's numba sieve drivers, i.e. everything
+ * below thewalrus/_hafnian.py:_haf / loop_hafnian and
+ * thewalrus/loop_hafnian_batch.py:loop_hafnian_batch.  Matrices are row-major; complex data is
+ * interleaved (re, im) doubles.  Host pointers unless stated otherwise.  Every entry point
+ * returns 0 on success or a negative WG_E* status; wg_last_error() describes the failure.
+ * There is no CPU fallback: without a usable GPU every call fails.
+ */
+#ifndef WALRUS_GB300_H
+#define WALRUS_GB300_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define WG_OK 0
+#define WG_EINVAL -1   /* bad argument, or a size beyond the kernels' limits */
+#define WG_ECUDA -2    /* CUDA runtime error (no device, launch failure, ...) */
+#define WG_ENOMEM -3   /* device or host allocation failed */
+#define WG_EKERNEL -4  /* a kernel reported an internal inconsistency */
+
+/* element type of matrix inputs */
+#define WG_FLOAT64 0
+#define WG_COMPLEX128 1
+
+/* arithmetic of the sieve terms */
+#define WG_PREC_FP64 0 /* FP64 throughout */
+#define WG_PREC_DF 1   /* FP32 double-float terms; FP64 pivots, divisions and accumulation */
+
+/* instance kinds for the batched interface */
+#define WG_KIND_PLAIN 0      /* _calc_hafnian */
+#define WG_KIND_LOOP 1       /* _calc_loop_hafnian (odd self-loop when has_odd) */
+#define WG_KIND_BATCH_EVEN 3 /* _calc_loop_hafnian_batch_even */
+#define WG_KIND_BATCH_ODD 4  /* _calc_loop_hafnian_batch_odd */
+
+/* One sieve problem, prepared exactly as the reference prepares the arguments of its numba
+ * drivers (thewalrus/_hafnian.py:415, :512; thewalrus/loop_hafnian_batch.py:51, :127). */
+typedef struct wg_instance {
+  int32_t kind;        /* WG_KIND_* */
+  int32_t n;           /* dimension of the prepared matrix A */
+  int32_t E;           /* entries of edge_reps (for batch kinds: the fixed edge reps) */
+  int32_t dtype;       /* WG_FLOAT64 or WG_COMPLEX128 for A, D, oddV */
+  int32_t glynn;       /* 1: finite-difference sieve; 0: inclusion/exclusion */
+  int32_t has_odd;     /* WG_KIND_LOOP: an odd self-loop is present */
+  int32_t batch_max;   /* batch kinds */
+  int32_t cutoff;      /* batch kinds: odd_cutoff (even kind) or even_cutoff (odd kind) */
+  const int64_t* edge_reps;
+  const void* A;       /* n x n */
+  const void* D;       /* n (loop and batch kinds) */
+  const void* oddV;    /* n (WG_KIND_LOOP with has_odd) */
+  double oddloop[2];   /* WG_KIND_LOOP with has_odd */
+} wg_instance;
+
+typedef struct wg_plan wg_plan;
+
+/* Select and initialise the CUDA device (optional: the first call initialises device 0). */
+int wg_init(int device);
+const char* wg_last_error(void);
+/* Number of output values of one instance (1, or the batch length). */
+int wg_instance_outputs(const wg_instance* inst);
+
+/* Replaces _calc_hafnian (thewalrus/_hafnian.py:415-467) as called from _haf (:505-507).
+ * A: prepared n x n matrix (n = 2E); out: {re, im}. */
+int wg_hafnian(const void* A, int n, int dtype, const int64_t* edge_reps, int E, int glynn, int precision,
+               double out[2], void* stream);
+
+/* Replaces _calc_loop_hafnian (thewalrus/_hafnian.py:511-577) as called from loop_hafnian
+ * (:627-630).  oddloop / oddV are read only when has_odd. */
+int wg_loop_hafnian(const void* A, const void* D, int n, int dtype, const int64_t* edge_reps, int E, int has_odd,
+                    const double oddloop[2], const void* oddV, int glynn, int precision, double out[2],
+                    void* stream);
+
+/* Replaces _calc_loop_hafnian_batch_even / _odd (thewalrus/loop_hafnian_batch.py:50-208) as
+ * called from loop_hafnian_batch (:294-304).  odd = 0: cutoff is odd_cutoff, output length
+ * 2*batch_max+cutoff+1; odd = 1: cutoff is even_cutoff, length 2*batch_max+cutoff+2.
+ * out: complex interleaved. */
+int wg_loop_hafnian_batch(const void* A, const void* D, int n, int dtype, const int64_t* fixed_edge_reps, int E,
+                          int batch_max, int cutoff, int odd, int glynn, int precision, double* out, void* stream);
+
+/* Batched interface: many instances of uneven size in one persistent launch per arithmetic
+ * class, with a device work queue over (instance, term range) chunks.  This has no single
+ * counterpart in the reference; it replaces a Python loop of _calc_* calls (the numba prange
+ * pool of thewalrus/_hafnian.py:443 spread over instances).
+ *   wg_plan_create : validate, prepare and upload the inputs, build the chunk queue
+ *   wg_plan_execute: launch the sieve and reduction kernels on `stream` (graph-capturable)
+ *   wg_plan_read   : copy all outputs (instance order, complex interleaved) to the host
+ * chunk_scale (>0) multiplies the default chunks-per-warp target (1.0 = default). */
+int wg_plan_create(const wg_instance* inst, int count, int precision, double chunk_scale, wg_plan** plan);
+int wg_plan_execute(wg_plan* plan, void* stream);
+int wg_plan_read(wg_plan* plan, double* out, void* stream);
+int wg_plan_outputs(const wg_plan* plan);
+int wg_plan_kernel_launches(const wg_plan* plan);
+int wg_plan_destroy(wg_plan* plan);
+/* create + execute + read + destroy */
+int wg_run(const wg_instance* inst, int count, int precision, double* out, void* stream);
+
+/* Device-time microbenchmark of the FP64 and FP32 FMA pipes (TFLOP/s, 2 flops per FMA). */
+int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

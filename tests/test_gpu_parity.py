@@ -1,0 +1,129 @@
+"""GPU parity: the CUDA sieve (through the C ABI) against vectors produced by the reference and
+against the CPU oracle in _Float128 arithmetic.  Tolerances: 1e-10 relative for FP64 terms;
+exact integer rounding where the hafnian is an integer below 2^53."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import thewalrus_gb300 as tw
+from thewalrus_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+T = [1, 1, 2, 4, 10, 26, 76, 232, 764, 2620, 9496]
+
+
+def rel(a, b):
+    return abs(complex(a) - complex(b)) / max(abs(complex(b)), 1e-300)
+
+
+def test_plain_vs_reference(golden):
+    for c in golden["haf"]:
+        got = tw.hafnian(c["A"])
+        assert isinstance(got, np.complex128)
+        assert rel(got, c["out"]) < RTOL, (c["A"].shape, got, c["out"])
+
+
+def test_inclexcl_vs_reference(golden):
+    for c in golden["haf_inclexcl"]:
+        assert rel(tw.hafnian(c["A"], method="inclexcl"), c["out"]) < RTOL
+
+
+def test_loop_vs_reference(golden):
+    for c in golden["lhaf"]:
+        got = tw.hafnian(c["A"], loop=True)
+        assert rel(got, c["out"]) < RTOL, (c["A"].shape, got, c["out"])
+
+
+def test_repeated_vs_reference(golden):
+    for c in golden["rep"]:
+        got = tw.hafnian_repeated(c["A"], list(c["rpt"]))
+        assert rel(got, c["out"]) < RTOL, (c["rpt"], got, c["out"])
+    for c in golden["rep_loop"]:
+        got = tw.hafnian_repeated(c["A"], list(c["rpt"]), mu=c["mu"], loop=True)
+        assert rel(got, c["out"]) < RTOL, (c["rpt"], got, c["out"])
+
+
+def test_batch_vs_reference(golden):
+    for c in golden["batch"]:
+        got = tw.loop_hafnian_batch(c["A"], c["D"], list(c["fixed"]), int(c["cutoff"]))
+        ref = c["out"]
+        assert got.shape == ref.shape
+        assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < RTOL
+
+
+def test_brute_force_small():
+    for n in (6, 8, 10):
+        A = wl.complex_symmetric(n, seed=70 + n)
+        assert rel(tw.hafnian(A), oracle.brute_hafnian(A)) < RTOL
+    for n in (5, 7, 9):
+        A = wl.complex_symmetric(n, seed=80 + n)
+        assert rel(tw.hafnian(A, loop=True), oracle.brute_hafnian(A, loop=True)) < RTOL
+
+
+@pytest.mark.parametrize("n", [6, 8, 12])
+def test_known_answers(n):
+    J = np.ones((2 * n, 2 * n))
+    assert tw.hafnian(J).real == math.factorial(2 * n) // (math.factorial(n) * 2**n)
+    O, B = np.zeros((n, n)), np.ones((n, n))
+    assert round(tw.hafnian(np.block([[O, B], [B, O]])).real) == math.factorial(n)
+    if n <= 10:
+        assert tw.hafnian(np.ones((n, n)), loop=True).real == pytest.approx(T[n], rel=1e-13)
+        assert tw.hafnian(np.ones((n + 1, n + 1)), loop=True).real == pytest.approx(T[n + 1], rel=1e-13)
+    assert tw.hafnian(np.identity(2 * n)) == 0
+    assert abs(tw.hafnian(np.identity(2 * n), loop=True) - 1) < 1e-12
+    assert tw.hafnian_repeated(np.array([[1.0]]), [2 * n]).real == pytest.approx(
+        math.factorial(2 * n) / (math.factorial(n) * 2**n), rel=1e-13)
+
+
+def test_all_ones_24_exact():
+    got = tw.hafnian(np.ones((24, 24)))
+    assert got.real == 316234143225.0 and got.imag == 0.0
+
+
+@pytest.mark.parametrize("n,kind", [(16, "complex"), (20, "signed"), (22, "nonneg"), (18, "adj")])
+def test_vs_quad_oracle(n, kind):
+    gen = {"complex": wl.complex_symmetric, "signed": wl.real_signed, "nonneg": wl.real_nonneg,
+           "adj": wl.adjacency01}[kind]
+    A = gen(n, seed=n)
+    ref = oracle.hafnian(A, precision="quad")
+    assert rel(tw.hafnian(A), ref) < RTOL
+    if kind == "adj":  # integer hafnian below 2^53: must round to the exact count
+        got = tw.hafnian(A)
+        assert round(got.real) == round(ref.real) and abs(got.real - round(ref.real)) < 1e-6
+
+
+def test_loop_odd_and_repeated_vs_quad():
+    A, gamma, rpt = wl.gaussian_state_loop(modes=8, seed=5, photons=16, max_rep=3)
+    ref = oracle.hafnian_repeated(A, list(rpt), mu=gamma, loop=True, precision="quad")
+    assert rel(tw.hafnian_repeated(A, list(rpt), mu=gamma, loop=True), ref) < RTOL
+    B = wl.complex_symmetric(13, seed=9)
+    assert rel(tw.hafnian(B, loop=True), oracle.hafnian(B, loop=True, precision="quad")) < RTOL
+
+
+def test_batch_identity():
+    # loop_hafnian_batch(A, D, fixed, c)[k] == loop_hafnian(A, D, reps=fixed + [k])
+    B, D, fixed, cutoff = wl.batch_loop_calls(count=1, seed=11, modes=6, cutoff=5)[0]
+    got = tw.loop_hafnian_batch(B, D, list(fixed), cutoff)
+    for k in range(cutoff + 1):
+        ref = oracle.loop_hafnian(B, D, list(fixed) + [k], precision="quad")
+        assert abs(got[k] - complex(ref)) <= RTOL * max(abs(complex(ref)), np.max(np.abs(got)) * 1e-3)
+
+
+def test_hafnian_batch_uneven():
+    mats = [wl.complex_symmetric(n, seed=n) for n in (6, 10, 14, 8)] + \
+        [wl.real_nonneg(n, seed=n) for n in (12, 16)]
+    got = tw.hafnian_batch(mats)
+    for A, g in zip(mats, got):
+        assert rel(g, tw.hafnian(A)) < 1e-13
+
+
+def test_inputs_not_mutated():
+    A = wl.complex_symmetric(10, seed=3)
+    A0 = A.copy()
+    tw.hafnian(A)
+    tw.hafnian(A, loop=True)
+    assert np.array_equal(A, A0)

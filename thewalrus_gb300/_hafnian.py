@@ -1,0 +1,311 @@
+"""Drop-in hafnian / loop-hafnian API on the GB300 sieve kernels.
+
+Same names, arguments, return conventions and errors as the reference's public functions:
+
+* ``hafnian``            thewalrus/_hafnian.py:717-818
+* ``hafnian_repeated``   thewalrus/_hafnian.py:864-936
+* ``loop_hafnian``       thewalrus/_hafnian.py:580-631
+* ``_haf``               thewalrus/_hafnian.py:470-508
+* ``input_validation``   thewalrus/_hafnian.py:634-665
+* ``reduction``          thewalrus/_hafnian.py:697-714
+* ``matched_reps``       thewalrus/_hafnian.py:80-159
+* ``loop_hafnian_batch`` thewalrus/loop_hafnian_batch.py:260-304
+
+The host keeps validation, the closed forms for tiny matrices, edge pairing and reordering;
+every sieve runs on the GPU (no CPU fallback).  Extra keyword ``precision`` selects "fp64"
+(default) or "df" (FP32 double-float term arithmetic).  Sieve results come back as
+``numpy.complex128`` also for real input, as in the reference.
+"""
+import numpy as np
+
+from . import _native as nat
+
+__all__ = [
+    "hafnian",
+    "hafnian_repeated",
+    "loop_hafnian",
+    "loop_hafnian_batch",
+    "hafnian_batch",
+    "input_validation",
+    "reduction",
+    "matched_reps",
+    "prepare_hafnian",
+    "prepare_loop_hafnian",
+    "prepare_loop_hafnian_batch",
+]
+
+DEFAULT_PRECISION = "fp64"
+
+
+def input_validation(A, rtol=1e-05, atol=1e-08):
+    """Checks that ``A`` is a square, NaN-free, symmetric NumPy array (raises otherwise)."""
+    if not isinstance(A, np.ndarray):
+        raise TypeError("Input matrix must be a NumPy array.")
+    n = A.shape
+    if n[0] != n[1]:
+        raise ValueError("Input matrix must be square.")
+    if np.isnan(A).any():
+        raise ValueError("Input matrix must not contain NaNs.")
+    if not np.allclose(A, A.T, rtol=rtol, atol=atol):
+        raise ValueError("Input matrix must be symmetric.")
+    return True
+
+
+def reduction(A, rpt):
+    """Repeat row/column i of ``A`` rpt[i] times (vectors: entry i)."""
+    rows = np.repeat(np.arange(len(rpt)), np.asarray(rpt, dtype=np.int64))
+    if A.ndim == 1:
+        return A[rows]
+    return A[:, rows][rows]
+
+
+def matched_reps(reps):
+    """Pair repeated indices into edges with multiplicities.
+
+    Greedy rule of the reference: repeatedly take the two indices with the most remaining
+    repetitions; if the largest has more than twice the second (or is alone) it is paired with
+    itself ``r // 2`` times, otherwise it is paired with the second as often as the second
+    allows.  Returns ``(x, edge_reps, oddmode)`` with vertex ``x[i]`` matched to ``x[i + E]``.
+    """
+    reps = [int(r) for r in reps]
+    if sum(reps) == 0:
+        return np.array([], dtype=int), np.array([], dtype=int), None
+    # (count, index) pairs, kept in descending order; ties broken by the larger index first
+    pool = sorted(((r, i) for i, r in enumerate(reps) if r > 0), reverse=True)
+    left, right, mult = [], [], []
+    while len(pool) > 1 or (pool and pool[0][0] > 1):
+        pool.sort(reverse=True)
+        top_r, top_i = pool[0]
+        if len(pool) == 1 or top_r > 2 * pool[1][0]:
+            left.append(top_i)
+            right.append(top_i)
+            mult.append(top_r // 2)
+            pool = pool[1:] if top_r % 2 == 0 else [(1, top_i)] + pool[1:]
+        else:
+            sec_r, sec_i = pool[1]
+            left.append(top_i)
+            right.append(sec_i)
+            mult.append(sec_r)
+            rest = pool[2:]
+            pool = [(top_r - sec_r, top_i)] + rest if top_r > sec_r else rest
+    oddmode = pool[0][1] if len(pool) == 1 else None
+    return np.asarray(left + right, dtype=np.int64), np.asarray(mult, dtype=np.int64), oddmode
+
+
+def _is_complex(*arrays):
+    return any(a is not None and np.iscomplexobj(a) for a in arrays)
+
+
+def prepare_hafnian(A, reps=None, glynn=True):
+    """Host preparation of ``_haf``: returns a native instance, or a plain value when the
+    sieve is not needed (no photons: 1.0; odd photon number: 0.0)."""
+    n = A.shape[0]
+    reps = [1] * n if reps is None else list(reps)
+    N = sum(reps)
+    if N == 0:
+        return 1.0
+    if N % 2 == 1:
+        return 0.0
+    assert n == len(reps)
+    x, edge_reps, _ = matched_reps(reps)
+    Ax = A[np.ix_(x, x)]
+    Ax = Ax.astype(np.complex128) if _is_complex(Ax) else Ax.astype(np.float64)
+    return nat.Instance(nat.WG_KIND_PLAIN, Ax, edge_reps, glynn=glynn)
+
+
+def prepare_loop_hafnian(A, D=None, reps=None, glynn=True):
+    """Host preparation of ``loop_hafnian``: native instance or a plain value."""
+    n = A.shape[0]
+    reps = [1] * n if reps is None else list(reps)
+    if D is None:
+        D = A.diagonal()
+    N = sum(reps)
+    if N == 0:
+        return 1.0
+    if N == 1:
+        return D[np.where(np.array(reps) == 1)[0][0]]
+    assert n == len(reps)
+    assert D.shape[0] == n
+    x, edge_reps, oddmode = matched_reps(reps)
+    cplx = _is_complex(A, D)
+    dt = np.complex128 if cplx else np.float64
+    if oddmode is not None:
+        oddloop = D[oddmode].astype(dt)
+        oddV = A[oddmode, x].astype(dt)
+    else:
+        oddloop, oddV = None, None
+    Ax = A[np.ix_(x, x)].astype(dt)
+    Dx = np.asarray(D)[x].astype(dt)
+    return nat.Instance(nat.WG_KIND_LOOP, Ax, edge_reps, glynn=glynn, D=Dx, oddV=oddV, oddloop=oddloop)
+
+
+def _finish(prep, precision):
+    if not isinstance(prep, nat.Instance):
+        return prep
+    return np.complex128(nat.run([prep], precision)[0])
+
+
+def _haf(A, reps=None, glynn=True, precision=None):
+    """Hafnian with optional repeated rows/columns (the reference's ``_haf``)."""
+    return _finish(prepare_hafnian(A, reps, glynn), precision or DEFAULT_PRECISION)
+
+
+def loop_hafnian(A, D=None, reps=None, glynn=True, precision=None):
+    """Loop hafnian with optional repeated rows/columns."""
+    return _finish(prepare_loop_hafnian(A, D, reps, glynn), precision or DEFAULT_PRECISION)
+
+
+def _closed_form(A, loop, rtol, atol):
+    """The reference's special cases of ``hafnian`` (empty, odd, diagonal, n <= 4);
+    returns (True, value) or (False, None)."""
+    matshape = A.shape
+    if matshape == (0, 0):
+        return True, 1
+    if matshape[0] % 2 != 0 and not loop:
+        return True, 0.0
+    if np.allclose(np.diag(np.diag(A)), A, rtol=rtol, atol=atol):
+        return True, (np.prod(np.diag(A)) if loop else 0)
+    if matshape[0] == 2:
+        return True, (A[0, 1] + A[0, 0] * A[1, 1] if loop else A[0][1])
+    if matshape[0] == 3 and loop:
+        return True, (A[0, 0] * A[1, 2] + A[1, 1] * A[0, 2] + A[2, 2] * A[0, 1]
+                      + A[0, 0] * A[1, 1] * A[2, 2])
+    if matshape[0] == 4:
+        if loop:
+            return True, (A[0, 1] * A[2, 3] + A[0, 2] * A[1, 3] + A[0, 3] * A[1, 2]
+                          + A[0, 0] * A[1, 1] * A[2, 3] + A[0, 1] * A[2, 2] * A[3, 3]
+                          + A[0, 2] * A[1, 1] * A[3, 3] + A[0, 0] * A[2, 2] * A[1, 3]
+                          + A[0, 0] * A[3, 3] * A[1, 2] + A[0, 3] * A[1, 1] * A[2, 2]
+                          + A[0, 0] * A[1, 1] * A[2, 2] * A[3, 3])
+        return True, A[0, 1] * A[2, 3] + A[0, 2] * A[1, 3] + A[0, 3] * A[1, 2]
+    return False, None
+
+
+def _method_glynn(method):
+    if method == "glynn":
+        return True
+    if method == "inclexcl":
+        return False
+    if method == "recursive":
+        raise NotImplementedError("method='recursive' is not part of the GPU sieve path")
+    raise ValueError("unknown hafnian method %r" % (method,))
+
+
+def hafnian(A, loop=False, rtol=1e-05, atol=1e-08, approx=False, num_samples=1000, method="glynn",
+            precision=None):
+    """Returns the hafnian (or loop hafnian) of a symmetric matrix.
+
+    Args and results as ``thewalrus.hafnian``; ``method`` is "glynn" or "inclexcl" (the loop
+    hafnian always uses the finite-difference sieve, as in the reference).
+    """
+    input_validation(A, rtol=rtol, atol=atol)
+    glynn = _method_glynn(method) if not loop else True
+    done, value = _closed_form(A, loop, rtol, atol)
+    if done:
+        return value
+    if approx:
+        raise NotImplementedError("approx=True (Barvinok sampling) is not part of the GPU sieve path")
+    if loop:
+        return loop_hafnian(A, D=None, reps=None, glynn=True, precision=precision)
+    return _haf(A, reps=None, glynn=glynn, precision=precision)
+
+
+def hafnian_repeated(A, rpt, mu=None, loop=False, rtol=1e-05, atol=1e-08, glynn=True, precision=None):
+    """Hafnian of ``A`` with row/column i repeated ``rpt[i]`` times (``mu``: loop weights)."""
+    input_validation(A, atol=atol, rtol=rtol)
+    if len(rpt) != len(A):
+        raise ValueError("the rpt argument must be 1-dimensional sequence of length len(A).")
+    nud = np.array(rpt, dtype=np.int32)
+    if not np.all(np.mod(rpt, 1) == 0) or np.any(nud < 0):
+        raise ValueError("the rpt argument must contain non-negative integers.")
+    if np.all(nud == 0):
+        return 1.0
+    if np.sum(nud) % 2 != 0 and not loop:
+        return 0.0
+    if mu is None:
+        mu = A.diagonal().copy()
+    if np.allclose(A, 0, rtol=rtol, atol=atol):
+        if loop:
+            return np.prod(mu**rpt)
+        return 0
+    if len(mu) != len(A):
+        raise ValueError("Length of means vector must be the same length as the matrix A.")
+    if loop:
+        return loop_hafnian(A, D=mu, reps=rpt, glynn=glynn, precision=precision)
+    return _haf(A, reps=rpt, glynn=glynn, precision=precision)
+
+
+def _batch_edges_even(fixed_edges):
+    if len(fixed_edges) == 0:
+        return np.array([0, 0], dtype=int)
+    half = fixed_edges.shape[0] // 2
+    new = int(max(fixed_edges)) + 1
+    return np.concatenate([[new], fixed_edges[:half], [new], fixed_edges[half:]]).astype(int)
+
+
+def _batch_edges_odd(fixed_edges, oddmode):
+    if len(fixed_edges) == 0:
+        return np.array([1, oddmode, 1, 1], dtype=int)
+    half = fixed_edges.shape[0] // 2
+    new = int(max(max(fixed_edges), oddmode)) + 1
+    return np.concatenate([[new, oddmode], fixed_edges[:half], [new, new], fixed_edges[half:]]).astype(int)
+
+
+def prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True):
+    """Host preparation of ``loop_hafnian_batch`` (loop_hafnian_batch.py:275-304)."""
+    n = A.shape[0]
+    assert A.shape[1] == n
+    assert D.shape == (n,)
+    assert len(fixed_reps) == n - 1
+    nz = np.nonzero(list(fixed_reps) + [1])[0]
+    Anz = A[np.ix_(nz, nz)]
+    Dnz = D[nz]
+    fixed_reps = np.asarray(fixed_reps)
+    fixed_reps_nz = fixed_reps[nz[:-1]]
+    fixed_edges, fixed_m_reps, oddmode = matched_reps(fixed_reps_nz)
+    dt = np.complex128 if _is_complex(A, D) else np.float64
+    if oddmode is None:
+        batch_max, cutoff, kind = N_cutoff // 2, N_cutoff % 2, nat.WG_KIND_BATCH_EVEN
+        edges = _batch_edges_even(fixed_edges)
+    else:
+        batch_max, cutoff, kind = (N_cutoff - 1) // 2, 1 - (N_cutoff % 2), nat.WG_KIND_BATCH_ODD
+        edges = _batch_edges_odd(fixed_edges, oddmode)
+    Ax = Anz[np.ix_(edges, edges)].astype(dt)
+    Dx = Dnz[edges].astype(dt)
+    return nat.Instance(kind, Ax, fixed_m_reps, glynn=glynn, D=Dx, batch_max=batch_max, cutoff=cutoff)
+
+
+def loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True, precision=None):
+    """Loop hafnians for every photon number 0..N_cutoff of the last mode, in one sieve."""
+    prep = prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn)
+    return nat.run([prep], precision or DEFAULT_PRECISION)
+
+
+def hafnian_batch(matrices, loop=False, rtol=1e-05, atol=1e-08, method="glynn", precision=None,
+                  validate=True):
+    """Hafnians of many matrices of uneven size in one persistent launch per arithmetic class.
+
+    Each result equals ``hafnian(M, loop=loop, method=method)``.  Instances that the reference
+    answers in closed form are answered the same way on the host; all others share one plan.
+    """
+    results = [None] * len(matrices)
+    insts, where = [], []
+    for i, A in enumerate(matrices):
+        if validate:
+            input_validation(A, rtol=rtol, atol=atol)
+        glynn = _method_glynn(method) if not loop else True
+        done, value = _closed_form(A, loop, rtol, atol)
+        if done:
+            results[i] = value
+            continue
+        prep = prepare_loop_hafnian(A, None, None, True) if loop else prepare_hafnian(A, None, glynn)
+        if isinstance(prep, nat.Instance):
+            insts.append(prep)
+            where.append(i)
+        else:
+            results[i] = prep
+    if insts:
+        vals = nat.run(insts, precision or DEFAULT_PRECISION)
+        for i, v in zip(where, vals):
+            results[i] = np.complex128(v)
+    return results

@@ -1,0 +1,258 @@
+// Scalar arithmetic for the sieve kernels.
+//
+// Four scalar types share one interface (struct Ar<S>):
+//   double  real FP64                 c64  complex FP64
+//   dfr     real double-float (FP32)  cdf  complex double-float
+// A double-float value is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), giving
+// a 48-bit significand from FP32 instructions only.  Products use the FMA error-free
+// transformation (err = fma(a, b, -a*b)); sums use Knuth's two-sum.  Conversions to and from
+// FP64 are exact for the hi part and round the lo part once.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wg {
+
+struct c64 {
+  double re, im;
+};
+struct dfr {
+  float hi, lo;
+};
+struct cdf {
+  dfr re, im;
+};
+
+__device__ __forceinline__ double neg_d(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ULL);
+}
+__device__ __forceinline__ float neg_f(float x) { return __int_as_float(__float_as_int(x) ^ 0x80000000); }
+__device__ __forceinline__ unsigned long long absbits_d(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ unsigned int absbits_f(float x) { return (unsigned)__float_as_int(x) & 0x7fffffffu; }
+
+// ---------------------------------------------------------------- double-float primitives
+__device__ __forceinline__ dfr df_two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ dfr df_fast_two_sum(float a, float b) {
+  float s = a + b;
+  float e = b - (s - a);
+  return {s, e};
+}
+__device__ __forceinline__ dfr df_add(dfr a, dfr b) {
+  dfr s = df_two_sum(a.hi, b.hi);
+  float lo = s.lo + (a.lo + b.lo);
+  return df_fast_two_sum(s.hi, lo);
+}
+__device__ __forceinline__ dfr df_neg(dfr a) { return {neg_f(a.hi), neg_f(a.lo)}; }
+__device__ __forceinline__ dfr df_mul(dfr a, dfr b) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  return df_fast_two_sum(p, e);
+}
+// c + a*b with one renormalisation
+__device__ __forceinline__ dfr df_fma(dfr a, dfr b, dfr c) {
+  float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, e);
+  e = fmaf(a.lo, b.hi, e);
+  dfr s = df_two_sum(c.hi, p);
+  float lo = s.lo + (c.lo + e);
+  return df_fast_two_sum(s.hi, lo);
+}
+// c + a*b + d*f  (two products accumulated before one renormalisation)
+__device__ __forceinline__ dfr df_fma2(dfr a, dfr b, dfr d, dfr f, dfr c) {
+  float p1 = a.hi * b.hi;
+  float e1 = fmaf(a.hi, b.hi, -p1);
+  e1 = fmaf(a.hi, b.lo, e1);
+  e1 = fmaf(a.lo, b.hi, e1);
+  float p2 = d.hi * f.hi;
+  float e2 = fmaf(d.hi, f.hi, -p2);
+  e2 = fmaf(d.hi, f.lo, e2);
+  e2 = fmaf(d.lo, f.hi, e2);
+  dfr s1 = df_two_sum(c.hi, p1);
+  dfr s2 = df_two_sum(s1.hi, p2);
+  float lo = (s1.lo + s2.lo) + (c.lo + (e1 + e2));
+  return df_fast_two_sum(s2.hi, lo);
+}
+__device__ __forceinline__ double df_to_d(dfr a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dfr df_from_d(double x) {
+  float h = __double2float_rn(x);
+  float l = __double2float_rn(x - (double)h);
+  return {h, l};
+}
+
+// ---------------------------------------------------------------- traits
+template <class S>
+struct Ar;
+
+template <>
+struct Ar<double> {
+  using S = double;
+  using Comp = double;  // reducible component type
+  static constexpr int NC = 1;
+  static constexpr bool cplx = false;
+  static constexpr bool fp64 = true;
+  __device__ static __forceinline__ S zero() { return 0.0; }
+  __device__ static __forceinline__ S one() { return 1.0; }
+  __device__ static __forceinline__ S add(S a, S b) { return a + b; }
+  __device__ static __forceinline__ S sub(S a, S b) { return a - b; }
+  __device__ static __forceinline__ S mul(S a, S b) { return a * b; }
+  __device__ static __forceinline__ S fma(S a, S b, S c) { return ::fma(a, b, c); }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) { return ::fma(neg_d(a), b, c); }
+  __device__ static __forceinline__ S neg(S a) { return neg_d(a); }
+  __device__ static __forceinline__ S conj(S a) { return a; }
+  __device__ static __forceinline__ S scale(S a, double s) { return a * s; }
+  __device__ static __forceinline__ S from_c64(c64 v) { return v.re; }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {a, 0.0}; }
+  __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a); }
+  __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a) == 0; }
+  __device__ static __forceinline__ S recip(S a) { return 1.0 / a; }
+  __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
+  __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) { a = v; }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return a + b; }
+  __device__ static __forceinline__ Comp shfl_xor(Comp v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+  __device__ static __forceinline__ S shfl(S v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+};
+
+template <>
+struct Ar<c64> {
+  using S = c64;
+  using Comp = double;
+  static constexpr int NC = 2;
+  static constexpr bool cplx = true;
+  static constexpr bool fp64 = true;
+  __device__ static __forceinline__ S zero() { return {0.0, 0.0}; }
+  __device__ static __forceinline__ S one() { return {1.0, 0.0}; }
+  __device__ static __forceinline__ S add(S a, S b) { return {a.re + b.re, a.im + b.im}; }
+  __device__ static __forceinline__ S sub(S a, S b) { return {a.re - b.re, a.im - b.im}; }
+  __device__ static __forceinline__ S mul(S a, S b) {
+    return {::fma(a.re, b.re, neg_d(a.im * b.im)), ::fma(a.re, b.im, a.im * b.re)};
+  }
+  // c + a*b : 4 DFMA
+  __device__ static __forceinline__ S fma(S a, S b, S c) {
+    return {::fma(a.re, b.re, ::fma(neg_d(a.im), b.im, c.re)), ::fma(a.re, b.im, ::fma(a.im, b.re, c.im))};
+  }
+  // c - a*b : 4 DFMA
+  __device__ static __forceinline__ S fnma(S a, S b, S c) {
+    return {::fma(neg_d(a.re), b.re, ::fma(a.im, b.im, c.re)), ::fma(neg_d(a.re), b.im, ::fma(neg_d(a.im), b.re, c.im))};
+  }
+  __device__ static __forceinline__ S neg(S a) { return {neg_d(a.re), neg_d(a.im)}; }
+  __device__ static __forceinline__ S conj(S a) { return {a.re, neg_d(a.im)}; }
+  __device__ static __forceinline__ S scale(S a, double s) { return {a.re * s, a.im * s}; }
+  __device__ static __forceinline__ S from_c64(c64 v) { return v; }
+  __device__ static __forceinline__ c64 to_c64(S a) { return a; }
+  __device__ static __forceinline__ unsigned long long key(S a) {
+    unsigned long long x = absbits_d(a.re), y = absbits_d(a.im);
+    return x > y ? x : y;
+  }
+  __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re) | absbits_d(a.im)) == 0; }
+  __device__ static __forceinline__ S recip(S a) {
+    double d = 1.0 / ::fma(a.re, a.re, a.im * a.im);
+    return {a.re * d, neg_d(a.im) * d};
+  }
+  __device__ static __forceinline__ Comp comp(const S& a, int i) { return i ? a.im : a.re; }
+  __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) {
+    if (i) a.im = v; else a.re = v;
+  }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return a + b; }
+  __device__ static __forceinline__ Comp shfl_xor(Comp v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+  __device__ static __forceinline__ S shfl(S v, int src) {
+    return {__shfl_sync(0xffffffffu, v.re, src), __shfl_sync(0xffffffffu, v.im, src)};
+  }
+};
+
+template <>
+struct Ar<dfr> {
+  using S = dfr;
+  using Comp = dfr;
+  static constexpr int NC = 1;
+  static constexpr bool cplx = false;
+  static constexpr bool fp64 = false;
+  __device__ static __forceinline__ S zero() { return {0.f, 0.f}; }
+  __device__ static __forceinline__ S one() { return {1.f, 0.f}; }
+  __device__ static __forceinline__ S add(S a, S b) { return df_add(a, b); }
+  __device__ static __forceinline__ S sub(S a, S b) { return df_add(a, df_neg(b)); }
+  __device__ static __forceinline__ S mul(S a, S b) { return df_mul(a, b); }
+  __device__ static __forceinline__ S fma(S a, S b, S c) { return df_fma(a, b, c); }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) { return df_fma(df_neg(a), b, c); }
+  __device__ static __forceinline__ S neg(S a) { return df_neg(a); }
+  __device__ static __forceinline__ S conj(S a) { return a; }
+  __device__ static __forceinline__ S scale(S a, double s) { return df_mul(a, df_from_d(s)); }
+  __device__ static __forceinline__ S from_c64(c64 v) { return df_from_d(v.re); }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a), 0.0}; }
+  __device__ static __forceinline__ unsigned long long key(S a) { return absbits_f(a.hi); }
+  __device__ static __forceinline__ bool is_zero(S a) { return absbits_f(a.hi) == 0; }
+  __device__ static __forceinline__ S recip(S a) { return df_from_d(1.0 / df_to_d(a)); }
+  __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
+  __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) { a = v; }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return df_add(a, b); }
+  __device__ static __forceinline__ Comp shfl_xor(Comp v, int m) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+  }
+  __device__ static __forceinline__ S shfl(S v, int src) {
+    return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+  }
+};
+
+template <>
+struct Ar<cdf> {
+  using S = cdf;
+  using Comp = dfr;
+  static constexpr int NC = 2;
+  static constexpr bool cplx = true;
+  static constexpr bool fp64 = false;
+  __device__ static __forceinline__ S zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
+  __device__ static __forceinline__ S one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
+  __device__ static __forceinline__ S add(S a, S b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
+  __device__ static __forceinline__ S sub(S a, S b) { return {df_add(a.re, df_neg(b.re)), df_add(a.im, df_neg(b.im))}; }
+  __device__ static __forceinline__ S mul(S a, S b) {
+    dfr z = {0.f, 0.f};
+    return {df_fma2(a.re, b.re, df_neg(a.im), b.im, z), df_fma2(a.re, b.im, a.im, b.re, z)};
+  }
+  __device__ static __forceinline__ S fma(S a, S b, S c) {
+    return {df_fma2(a.re, b.re, df_neg(a.im), b.im, c.re), df_fma2(a.re, b.im, a.im, b.re, c.im)};
+  }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) {
+    return {df_fma2(df_neg(a.re), b.re, a.im, b.im, c.re), df_fma2(df_neg(a.re), b.im, df_neg(a.im), b.re, c.im)};
+  }
+  __device__ static __forceinline__ S neg(S a) { return {df_neg(a.re), df_neg(a.im)}; }
+  __device__ static __forceinline__ S conj(S a) { return {a.re, df_neg(a.im)}; }
+  __device__ static __forceinline__ S scale(S a, double s) {
+    dfr t = df_from_d(s);
+    return {df_mul(a.re, t), df_mul(a.im, t)};
+  }
+  __device__ static __forceinline__ S from_c64(c64 v) { return {df_from_d(v.re), df_from_d(v.im)}; }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a.re), df_to_d(a.im)}; }
+  __device__ static __forceinline__ unsigned long long key(S a) {
+    unsigned x = absbits_f(a.re.hi), y = absbits_f(a.im.hi);
+    return x > y ? x : y;
+  }
+  __device__ static __forceinline__ bool is_zero(S a) { return (absbits_f(a.re.hi) | absbits_f(a.im.hi)) == 0; }
+  __device__ static __forceinline__ S recip(S a) {
+    c64 z = to_c64(a);
+    double d = 1.0 / ::fma(z.re, z.re, z.im * z.im);
+    return from_c64({z.re * d, -z.im * d});
+  }
+  __device__ static __forceinline__ Comp comp(const S& a, int i) { return i ? a.im : a.re; }
+  __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) {
+    if (i) a.im = v; else a.re = v;
+  }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return df_add(a, b); }
+  __device__ static __forceinline__ Comp shfl_xor(Comp v, int m) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+  }
+  __device__ static __forceinline__ S shfl(S v, int src) {
+    return {{__shfl_sync(0xffffffffu, v.re.hi, src), __shfl_sync(0xffffffffu, v.re.lo, src)},
+            {__shfl_sync(0xffffffffu, v.im.hi, src), __shfl_sync(0xffffffffu, v.im.lo, src)}};
+  }
+};
+
+}  // namespace wg

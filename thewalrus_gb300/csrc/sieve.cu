@@ -1,0 +1,743 @@
+// Host runtime and C ABI of the hafnian sieve (see include/walrus_gb300.h).
+//
+// A plan turns a list of prepared instances into
+//   * one device pool holding each instance's extended matrix [[A, D], [D^T, 0], [oddV], [oddV0]]
+//     converted to the kernel's scalar type,
+//   * a chunk queue: every instance's term range split into chunks whose cost is balanced
+//     against the number of resident warps, largest instances first,
+//   * one persistent sieve launch per (scalar type, register class) group, and one reduction
+//     launch that sums chunk partials in a fixed order (bitwise reproducible results).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/walrus_gb300.h"
+#include "sieve_kernel.cuh"
+
+namespace wg {
+
+static thread_local std::string g_err;
+static int g_device = -1;
+static int g_num_sms = 0;
+static std::mutex g_init_mu;
+
+static int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess) return fail(WG_ECUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), \
+                                       __FILE__, __LINE__);                                     \
+  } while (0)
+
+static int ensure_init(int device) {
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (g_device >= 0 && (device < 0 || device == g_device)) {
+    CK(cudaSetDevice(g_device));
+    return WG_OK;
+  }
+  int dev = device < 0 ? 0 : device;
+  int count = 0;
+  CK(cudaGetDeviceCount(&count));
+  if (count <= 0) return fail(WG_ECUDA, "no CUDA device");
+  if (dev >= count) return fail(WG_EINVAL, "device %d not present (%d devices)", dev, count);
+  CK(cudaSetDevice(dev));
+  CK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+  // constant tables: binomials and reciprocals
+  static double binom[BINOM_N][BINOM_N];
+  for (int i = 0; i < BINOM_N; ++i)
+    for (int j = 0; j < BINOM_N; ++j) {
+      if (j > i) { binom[i][j] = 0; continue; }
+      long double b = 1;
+      for (int q = 0; q < j; ++q) b = b * (long double)(i - q) / (long double)(q + 1);
+      binom[i][j] = (double)std::llround((double)b) == (double)b ? (double)b : (double)b;
+    }
+  double inv[256];
+  inv[0] = 0;
+  for (int k = 1; k < 256; ++k) inv[k] = 1.0 / (double)k;
+  CK(cudaMemcpyToSymbol(c_binom, binom, sizeof(binom)));
+  CK(cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)));
+  g_device = dev;
+  return WG_OK;
+}
+
+// scalar classes
+enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3 };
+static size_t stype_bytes(int st) { return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16; }
+
+struct Prepared {
+  InstDev d;
+  int stype;
+  int rows_max, mb_max, m_max, kc_max, nser_need, narr;
+  double term_cost;
+  std::vector<double> scales;
+  std::vector<unsigned char> ext;  // extended matrix in the kernel's scalar type
+};
+
+struct Group {
+  int stype, ns;
+  WarpLayout L;
+  int wpc, ctas;
+  int chunk_begin, chunk_count;
+};
+
+}  // namespace wg
+
+struct wg_plan {
+  std::vector<wg::InstDev> inst;
+  std::vector<wg::ChunkDev> chunks;
+  std::vector<wg::Group> groups;
+  int total_out = 0;
+  int nparts = 0;
+  int precision = 0;
+  void* dmem = nullptr;
+  wg::InstDev* d_inst = nullptr;
+  wg::ChunkDev* d_chunks = nullptr;
+  unsigned char* d_pool = nullptr;
+  double2* d_partials = nullptr;
+  double* d_scales = nullptr;
+  double2* d_out = nullptr;
+  unsigned int* d_counters = nullptr;
+  int* d_err = nullptr;
+};
+
+namespace wg {
+
+static const int NS_CPLX[] = {4, 6, 8, 10};
+static const int NS_REAL[] = {4, 8, 12};
+
+template <class S, int NS>
+static cudaError_t launch_one(const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
+  auto k = sieve_kernel<S, NS>;
+  const int smem = wpc * p.L.bytes;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  k<<<ctas, 32 * wpc, smem, st>>>(p);
+  return cudaGetLastError();
+}
+
+template <class S, int NS>
+static int occupancy_one(int wpc, int smem) {
+  int nb = 0;
+  auto k = sieve_kernel<S, NS>;
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpc, smem) != cudaSuccess) return 0;
+  return nb;
+}
+
+#define WG_DISPATCH(ST, NS, CALL)                              \
+  switch (ST) {                                                \
+    case ST_CPLX64:                                            \
+      switch (NS) {                                            \
+        case 4: CALL(c64, 4); break;                           \
+        case 6: CALL(c64, 6); break;                           \
+        case 8: CALL(c64, 8); break;                           \
+        default: CALL(c64, 10); break;                         \
+      }                                                        \
+      break;                                                   \
+    case ST_CPLXDF:                                            \
+      switch (NS) {                                            \
+        case 4: CALL(cdf, 4); break;                           \
+        case 6: CALL(cdf, 6); break;                           \
+        case 8: CALL(cdf, 8); break;                           \
+        default: CALL(cdf, 10); break;                         \
+      }                                                        \
+      break;                                                   \
+    case ST_REAL64:                                            \
+      switch (NS) {                                            \
+        case 4: CALL(double, 4); break;                        \
+        case 8: CALL(double, 8); break;                        \
+        default: CALL(double, 12); break;                      \
+      }                                                        \
+      break;                                                   \
+    default:                                                   \
+      switch (NS) {                                            \
+        case 4: CALL(dfr, 4); break;                           \
+        case 8: CALL(dfr, 8); break;                           \
+        default: CALL(dfr, 12); break;                         \
+      }                                                        \
+      break;                                                   \
+  }
+
+static int pick_ns(int stype, int rows) {
+  if (stype == ST_CPLX64 || stype == ST_CPLXDF) {
+    for (int ns : NS_CPLX)
+      if (8 * ns >= rows) return ns;
+  } else {
+    for (int ns : NS_REAL)
+      if (8 * ns >= rows) return ns;
+  }
+  return -1;
+}
+
+static inline void put_scalar(unsigned char* dst, int st, double re, double im) {
+  switch (st) {
+    case ST_REAL64: memcpy(dst, &re, 8); break;
+    case ST_CPLX64: memcpy(dst, &re, 8); memcpy(dst + 8, &im, 8); break;
+    case ST_REALDF: {
+      float h = (float)re, l = (float)(re - (double)h);
+      memcpy(dst, &h, 4); memcpy(dst + 4, &l, 4);
+      break;
+    }
+    default: {
+      float h = (float)re, l = (float)(re - (double)h);
+      float hi = (float)im, li = (float)(im - (double)hi);
+      memcpy(dst, &h, 4); memcpy(dst + 4, &l, 4); memcpy(dst + 8, &hi, 4); memcpy(dst + 12, &li, 4);
+      break;
+    }
+  }
+}
+
+static inline void get_val(const void* p, int dtype, size_t idx, double& re, double& im) {
+  const double* d = (const double*)p;
+  if (dtype == WG_COMPLEX128) { re = d[2 * idx]; im = d[2 * idx + 1]; }
+  else { re = d[idx]; im = 0.0; }
+}
+
+static int prepare(const wg_instance& in, int precision, Prepared& P) {
+  memset(&P.d, 0, sizeof(P.d));
+  InstDev& d = P.d;
+  if (in.dtype != WG_FLOAT64 && in.dtype != WG_COMPLEX128) return fail(WG_EINVAL, "dtype must be WG_FLOAT64 or WG_COMPLEX128");
+  if (in.n < 0 || in.E < 0) return fail(WG_EINVAL, "negative size");
+  if (in.n > 0 && !in.A) return fail(WG_EINVAL, "A is NULL");
+  std::vector<int> reps;
+  int kind = in.kind;
+  int nb = 0, ne = 0;
+  if (kind == WG_KIND_PLAIN || kind == WG_KIND_LOOP) {
+    if (in.n != 2 * in.E) return fail(WG_EINVAL, "prepared matrix must be 2E x 2E (n=%d, E=%d)", in.n, in.E);
+    for (int i = 0; i < in.E; ++i) reps.push_back((int)in.edge_reps[i]);
+    if (kind == WG_KIND_LOOP) {
+      nb = 1;
+      if (!in.D) return fail(WG_EINVAL, "D is NULL");
+      if (in.has_odd) {
+        ne = 1;
+        if (!in.oddV) return fail(WG_EINVAL, "oddV is NULL");
+        kind = KIND_LOOP_ODD;
+      }
+    }
+  } else if (kind == WG_KIND_BATCH_EVEN || kind == WG_KIND_BATCH_ODD) {
+    const bool odd = kind == WG_KIND_BATCH_ODD;
+    const int nbe = odd ? 2 : 1;
+    if (in.n != 2 * (in.E + nbe)) return fail(WG_EINVAL, "batch matrix must be 2(E+%d) square", nbe);
+    if (!in.D) return fail(WG_EINVAL, "D is NULL");
+    if (in.batch_max < 0 || in.cutoff < 0 || in.cutoff > 1) return fail(WG_EINVAL, "bad batch_max / cutoff");
+    reps.push_back(in.batch_max);
+    if (odd) reps.push_back(1);
+    for (int i = 0; i < in.E; ++i) reps.push_back((int)in.edge_reps[i]);
+    nb = 1;
+    ne = odd ? 2 : 1;
+  } else {
+    return fail(WG_EINVAL, "unknown kind %d", in.kind);
+  }
+  const int E = (int)reps.size();
+  if (E > MAX_EDGES) return fail(WG_EINVAL, "at most %d edges per sieve (got %d)", MAX_EDGES, E);
+  long long sumr = 0;
+  int maxr = 0;
+  for (int r : reps) {
+    if (r < 0) return fail(WG_EINVAL, "negative edge repetition");
+    if (r > BINOM_N - 1) return fail(WG_EINVAL, "edge repetition %d above the supported %d", r, BINOM_N - 1);
+    sumr += r;
+    maxr = std::max(maxr, r);
+  }
+  d.kind = kind;
+  d.n = in.n;
+  d.E = E;
+  d.glynn = in.glynn ? 1 : 0;
+  d.nb = nb;
+  d.ne = ne;
+  d.lda = in.n + 1;
+  d.unit_binoms = maxr <= 1;
+  int nout = 1;
+  double alpha = 1.0;  // input prescale (double-float only): A -> alpha A, D -> sqrt(alpha) D
+  if (precision == WG_PREC_DF) {
+    double rs = 0;
+    for (int i = 0; i < in.n; ++i) {
+      double s = 0, re, im;
+      for (int j = 0; j < in.n; ++j) { get_val(in.A, in.dtype, (size_t)i * in.n + j, re, im); s += std::hypot(re, im); }
+      rs = std::max(rs, s);
+    }
+    if (rs > 0 && std::isfinite(rs)) alpha = std::exp2(-std::round(std::log2(rs)));
+  }
+  const double salpha = std::sqrt(alpha);
+  int Nf = 0;
+  if (kind == KIND_PLAIN || kind == KIND_LOOP) {
+    d.N = (int)(2 * sumr);
+    d.K = d.N / 2;
+    d.Nodd = 0;
+    d.half_first = d.glynn;
+    const int e = d.glynn ? d.N / 2 - 1 : 0;
+    P.scales.push_back(std::ldexp(1.0, -e) * std::pow(alpha, -0.5 * d.N));
+  } else if (kind == KIND_LOOP_ODD) {
+    d.N = (int)(2 * sumr + 1);
+    d.K = d.N / 2;
+    d.Nodd = d.N;
+    d.half_first = 0;
+    const int e = d.glynn ? d.N / 2 : 0;
+    P.scales.push_back(std::ldexp(1.0, -e) * std::pow(alpha, -0.5 * d.N));
+    d.oddloop = {in.oddloop[0] * salpha, in.oddloop[1] * salpha};
+  } else {
+    const bool odd = kind == KIND_BATCH_ODD;
+    long long sf = 0;
+    for (int i = 0; i < in.E; ++i) sf += in.edge_reps[i];
+    Nf = (int)(2 * sf + (odd ? 1 : 0));
+    const int Nmax = odd ? Nf + 2 * in.batch_max + in.cutoff + 1 : Nf + 2 * in.batch_max + in.cutoff;
+    nout = odd ? 2 * in.batch_max + in.cutoff + 2 : 2 * in.batch_max + in.cutoff + 1;
+    if (nout > 32) return fail(WG_EINVAL, "batch output length %d above 32", nout);
+    d.N = Nf;
+    d.K = Nmax / 2;
+    d.Nodd = Nmax;
+    d.batch_max = in.batch_max;
+    d.half_first = 0;
+    double re, im;
+    get_val(in.D, in.dtype, 0, re, im);
+    d.oddloop = {re * salpha, im * salpha};
+    if (odd) {
+      get_val(in.D, in.dtype, 1, re, im);
+      d.oddloop0 = {re * salpha, im * salpha};
+    }
+    for (int o = 0; o < nout; ++o) {
+      const int x = Nf + o;
+      P.scales.push_back((d.glynn ? std::ldexp(1.0, -(x / 2)) : 1.0) * std::pow(alpha, -0.5 * x));
+    }
+  }
+  d.nout = nout;
+  long long steps = 1;
+  for (int i = 0; i < E; ++i) {
+    const int R = (i == 0 && d.half_first) ? (reps[0] + 2) / 2 : reps[i] + 1;
+    d.radix[i] = R;
+    d.reps[i] = reps[i];
+    if (steps > (1LL << 62) / R) return fail(WG_EINVAL, "too many sieve terms");
+    steps *= R;
+  }
+  d.steps = steps;
+  // term matrix size bounds
+  const int m_max = 2 * (int)std::count_if(reps.begin(), reps.end(), [](int r) { return r > 0; });
+  P.m_max = m_max;
+  P.mb_max = m_max + nb;
+  P.rows_max = m_max + nb + ne;
+  P.kc_max = std::min(d.K, m_max);
+  P.nser_need = std::max(std::max(d.K, d.Nodd), std::max(Nf, m_max)) + 2;
+  P.narr = (kind == KIND_PLAIN) ? 2 : 8;
+  P.term_cost = (double)P.mb_max * P.mb_max * P.mb_max + 64.0;
+  if (P.rows_max > 80) return fail(WG_EINVAL, "term matrix of %d rows above the supported 80", P.rows_max);
+  if (P.kc_max > 64) return fail(WG_EINVAL, "more than 64 characteristic coefficients");
+  if (d.Nodd > 250 || d.K > 250) return fail(WG_EINVAL, "photon number above the supported 250");
+  const bool cplx = in.dtype == WG_COMPLEX128;
+  P.stype = precision == WG_PREC_DF ? (cplx ? ST_CPLXDF : ST_REALDF) : (cplx ? ST_CPLX64 : ST_REAL64);
+  // extended matrix [[A, D], [D^T, 0], [oddV, 0], [oddV0, 0]]  ((n+3) x (n+1))
+  const int n = in.n, lda = n + 1;
+  const size_t sb = stype_bytes(P.stype);
+  P.ext.assign((size_t)(n + 3) * lda * sb, 0);
+  auto at = [&](int r, int c) { return P.ext.data() + ((size_t)r * lda + c) * sb; };
+  double re, im;
+  for (int r = 0; r < n; ++r)
+    for (int c = 0; c < n; ++c) {
+      get_val(in.A, in.dtype, (size_t)r * n + c, re, im);
+      put_scalar(at(r, c), P.stype, re * alpha, im * alpha);
+    }
+  if (nb) {
+    for (int i = 0; i < n; ++i) {
+      get_val(in.D, in.dtype, i, re, im);
+      put_scalar(at(i, n), P.stype, re * salpha, im * salpha);
+      put_scalar(at(n, i), P.stype, re * salpha, im * salpha);
+    }
+  }
+  if (kind == KIND_LOOP_ODD) {
+    for (int i = 0; i < n; ++i) {
+      get_val(in.oddV, in.dtype, i, re, im);
+      put_scalar(at(n + 1, i), P.stype, re * alpha, im * alpha);
+    }
+  }
+  if (kind == KIND_BATCH_EVEN || kind == KIND_BATCH_ODD) {
+    for (int i = 0; i < n; ++i) {  // oddV = A[0, :]
+      get_val(in.A, in.dtype, (size_t)i, re, im);
+      put_scalar(at(n + 1, i), P.stype, re * alpha, im * alpha);
+    }
+    if (kind == KIND_BATCH_ODD)
+      for (int i = 0; i < n; ++i) {  // oddV0 = A[1, :]
+        get_val(in.A, in.dtype, (size_t)n + i, re, im);
+        put_scalar(at(n + 2, i), P.stype, re * alpha, im * alpha);
+      }
+  }
+  return WG_OK;
+}
+
+static WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int narr) {
+  WarpLayout L;
+  const int sb = (int)stype_bytes(stype);
+  auto al = [](int x) { return (x + 15) & ~15; };
+  L.ldw = std::max(mb, 1) | 1;
+  L.rows = std::max(rows, 1);
+  L.kw = kc + 1;
+  L.nser = (nser + 1) & ~1;
+  int off = al(L.rows * L.ldw * sb);
+  L.off_x = off;
+  off += al(L.ldw * sb);
+  L.off_win = off;
+  off += al(L.kw * L.kw * sb);
+  L.off_ser = off;
+  off += al(narr * L.nser * sb);
+  L.off_int = off;
+  off += al((L.rows + 2 * L.ldw) * 4);
+  L.bytes = al(off);
+  return L;
+}
+
+static int build_plan(const wg_instance* v, int count, int precision, double chunk_scale, wg_plan* pl) {
+  if (count < 0 || (count > 0 && !v)) return fail(WG_EINVAL, "bad instance list");
+  if (precision != WG_PREC_FP64 && precision != WG_PREC_DF) return fail(WG_EINVAL, "unknown precision %d", precision);
+  if (!(chunk_scale > 0)) chunk_scale = 1.0;
+  std::vector<Prepared> P(count);
+  for (int i = 0; i < count; ++i) {
+    int rc = prepare(v[i], precision, P[i]);
+    if (rc) return fail(rc, "instance %d: %s", i, g_err.c_str());
+  }
+  pl->precision = precision;
+  // outputs and scales in instance order
+  int out = 0;
+  std::vector<double> scales;
+  for (int i = 0; i < count; ++i) {
+    P[i].d.out_base = out;
+    P[i].d.scale_base = (int)scales.size();
+    out += P[i].d.nout;
+    scales.insert(scales.end(), P[i].scales.begin(), P[i].scales.end());
+  }
+  pl->total_out = out;
+  // groups by (stype, ns)
+  struct GKey { int st, ns; };
+  std::vector<GKey> keys;
+  std::vector<int> gid(count);
+  for (int i = 0; i < count; ++i) {
+    const int ns = pick_ns(P[i].stype, P[i].rows_max);
+    if (ns < 0) return fail(WG_EINVAL, "instance %d: term matrix too large", i);
+    int g = -1;
+    for (size_t k = 0; k < keys.size(); ++k)
+      if (keys[k].st == P[i].stype && keys[k].ns == ns) g = (int)k;
+    if (g < 0) { keys.push_back({P[i].stype, ns}); g = (int)keys.size() - 1; }
+    gid[i] = g;
+  }
+  // pool
+  size_t pool_bytes = 0;
+  for (int i = 0; i < count; ++i) {
+    P[i].d.a_off = (long long)pool_bytes;
+    pool_bytes += (P[i].ext.size() + 255) & ~(size_t)255;
+  }
+  int nparts = 0;
+  for (size_t g = 0; g < keys.size(); ++g) {
+    Group G;
+    G.stype = keys[g].st;
+    G.ns = keys[g].ns;
+    int rows = 1, mb = 1, kc = 0, nser = 2, narr = 2;
+    double total_cost = 0;
+    std::vector<int> members;
+    for (int i = 0; i < count; ++i)
+      if (gid[i] == (int)g) {
+        members.push_back(i);
+        rows = std::max(rows, P[i].rows_max);
+        mb = std::max(mb, P[i].mb_max);
+        kc = std::max(kc, P[i].kc_max);
+        nser = std::max(nser, P[i].nser_need);
+        narr = std::max(narr, P[i].narr);
+        total_cost += P[i].term_cost * (double)P[i].d.steps;
+      }
+    G.L = make_layout(G.stype, rows, mb, kc, nser, narr);
+    const int max_smem = 227 * 1024;
+    int wpc = std::min(8, max_smem / G.L.bytes);
+    if (wpc < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
+    int per_sm = 0;
+#define WG_OCC(S, NS) per_sm = occupancy_one<S, NS>(wpc, wpc * G.L.bytes)
+    WG_DISPATCH(G.stype, G.ns, WG_OCC)
+#undef WG_OCC
+    if (per_sm < 1) {
+      cudaGetLastError();
+      return fail(WG_ECUDA, "sieve kernel cannot be resident (workspace %d B x %d warps)", G.L.bytes, wpc);
+    }
+    G.wpc = wpc;
+    const long long resident = (long long)g_num_sms * per_sm * wpc;
+    // chunking: about 4 chunks per resident warp (scaled), largest instances first
+    const double target = std::max(1.0, total_cost / (double)(resident * 4.0 * chunk_scale));
+    std::stable_sort(members.begin(), members.end(), [&](int a, int b) {
+      return P[a].term_cost * (double)P[a].d.steps > P[b].term_cost * (double)P[b].d.steps;
+    });
+    G.chunk_begin = (int)pl->chunks.size();
+    for (int i : members) {
+      InstDev& d = P[i].d;
+      long long per = (long long)std::max(1.0, std::floor(target / P[i].term_cost));
+      if (per > d.steps) per = d.steps;
+      const long long nch = (d.steps + per - 1) / per;
+      d.part_base = nparts;
+      d.nchunks = (int)nch;
+      for (long long c = 0; c < nch; ++c) {
+        ChunkDev ch;
+        ch.inst = i;
+        ch.part = nparts + (int)c * d.nout;
+        ch.t0 = d.steps * c / nch;
+        ch.t1 = d.steps * (c + 1) / nch;
+        pl->chunks.push_back(ch);
+      }
+      nparts += (int)nch * d.nout;
+    }
+    G.chunk_count = (int)pl->chunks.size() - G.chunk_begin;
+    G.ctas = (int)std::min<long long>((long long)g_num_sms * per_sm, (G.chunk_count + wpc - 1) / wpc);
+    G.ctas = std::max(G.ctas, 1);
+    pl->groups.push_back(G);
+  }
+  pl->nparts = nparts;
+  for (int i = 0; i < count; ++i) pl->inst.push_back(P[i].d);
+  // one device allocation
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t b_inst = al(sizeof(InstDev) * std::max(count, 1));
+  const size_t b_chunks = al(sizeof(ChunkDev) * std::max<size_t>(pl->chunks.size(), 1));
+  const size_t b_pool = al(std::max<size_t>(pool_bytes, 16));
+  const size_t b_parts = al(sizeof(double2) * std::max(nparts, 1));
+  const size_t b_scales = al(sizeof(double) * std::max<size_t>(scales.size(), 1));
+  const size_t b_out = al(sizeof(double2) * std::max(out, 1));
+  const size_t b_cnt = al(sizeof(unsigned int) * std::max<size_t>(pl->groups.size(), 1));
+  const size_t b_err = al(sizeof(int));
+  const size_t total = b_inst + b_chunks + b_pool + b_parts + b_scales + b_out + b_cnt + b_err;
+  if (cudaMalloc(&pl->dmem, total) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(WG_ENOMEM, "cudaMalloc of %zu bytes failed", total);
+  }
+  unsigned char* base = (unsigned char*)pl->dmem;
+  pl->d_inst = (InstDev*)base; base += b_inst;
+  pl->d_chunks = (ChunkDev*)base; base += b_chunks;
+  pl->d_pool = base; base += b_pool;
+  pl->d_partials = (double2*)base; base += b_parts;
+  pl->d_scales = (double*)base; base += b_scales;
+  pl->d_out = (double2*)base; base += b_out;
+  pl->d_counters = (unsigned int*)base; base += b_cnt;
+  pl->d_err = (int*)base;
+  // staging: one host buffer with the same layout for the upload
+  std::vector<unsigned char> host(b_inst + b_chunks + b_pool + b_parts + b_scales, 0);
+  memcpy(host.data(), pl->inst.data(), sizeof(InstDev) * count);
+  if (!pl->chunks.empty()) memcpy(host.data() + b_inst, pl->chunks.data(), sizeof(ChunkDev) * pl->chunks.size());
+  for (int i = 0; i < count; ++i)
+    memcpy(host.data() + b_inst + b_chunks + P[i].d.a_off, P[i].ext.data(), P[i].ext.size());
+  if (!scales.empty()) memcpy(host.data() + b_inst + b_chunks + b_pool + b_parts, scales.data(), sizeof(double) * scales.size());
+  CK(cudaMemcpy(pl->dmem, host.data(), host.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemset(pl->d_counters, 0, b_cnt + b_err));
+  return WG_OK;
+}
+
+static int execute_plan(wg_plan* pl, cudaStream_t st) {
+  for (size_t g = 0; g < pl->groups.size(); ++g) {
+    const Group& G = pl->groups[g];
+    SieveParams p;
+    p.inst = pl->d_inst;
+    p.chunks = pl->d_chunks + G.chunk_begin;
+    p.nchunks = G.chunk_count;
+    p.pool = pl->d_pool;
+    p.partials = pl->d_partials;
+    p.counter = pl->d_counters + g;
+    p.err = pl->d_err;
+    p.L = G.L;
+    cudaError_t e = cudaSuccess;
+#define WG_LAUNCH(S, NS) e = launch_one<S, NS>(p, G.ctas, G.wpc, st)
+    WG_DISPATCH(G.stype, G.ns, WG_LAUNCH)
+#undef WG_LAUNCH
+    if (e != cudaSuccess) return fail(WG_ECUDA, "sieve launch: %s", cudaGetErrorString(e));
+  }
+  const int ninst = (int)pl->inst.size();
+  if (ninst > 0) {
+    const int threads = 128;
+    const int blocks = (pl->total_out + threads - 1) / threads;
+    reduce_kernel<<<std::max(blocks, 1), threads, 0, st>>>(pl->d_inst, ninst, pl->d_partials, pl->d_scales, pl->d_out,
+                                                           pl->d_counters, (int)pl->groups.size(), pl->total_out);
+    CK(cudaGetLastError());
+  }
+  return WG_OK;
+}
+
+static void destroy_plan(wg_plan* pl) {
+  if (!pl) return;
+  if (pl->dmem) cudaFree(pl->dmem);
+  delete pl;
+}
+
+// ---------------------------------------------------------------- FP pipe microbenchmark
+template <typename T>
+__global__ void fma_peak_kernel(T* out, int iters, T a, T b) {
+  T x[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) x[c] = (T)(threadIdx.x + c);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) x[c] = x[c] * a + b;
+  }
+  T s = 0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += x[c];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+template <typename T>
+static int time_peak(int blocks, int threads, int iters, double* tflops) {
+  T* buf = nullptr;
+  CK(cudaMalloc(&buf, sizeof(T) * blocks * threads));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 4; ++rep) {
+    CK(cudaEventRecord(e0));
+    fma_peak_kernel<T><<<blocks, threads>>>(buf, iters, (T)0.999999, (T)1e-7);
+    CK(cudaEventRecord(e1));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0) best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  *tflops = 2.0 * 8.0 * (double)blocks * threads * (double)iters / (best * 1e-3) / 1e12;
+  return WG_OK;
+}
+
+}  // namespace wg
+
+using namespace wg;
+
+extern "C" {
+
+int wg_init(int device) { return ensure_init(device); }
+
+const char* wg_last_error(void) { return g_err.c_str(); }
+
+int wg_instance_outputs(const wg_instance* in) {
+  if (!in) return fail(WG_EINVAL, "NULL instance");
+  if (in->kind == WG_KIND_BATCH_EVEN) return 2 * in->batch_max + in->cutoff + 1;
+  if (in->kind == WG_KIND_BATCH_ODD) return 2 * in->batch_max + in->cutoff + 2;
+  return 1;
+}
+
+int wg_plan_create(const wg_instance* inst, int count, int precision, double chunk_scale, wg_plan** plan) {
+  if (!plan) return fail(WG_EINVAL, "plan is NULL");
+  *plan = nullptr;
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  wg_plan* pl = new wg_plan();
+  rc = build_plan(inst, count, precision, chunk_scale, pl);
+  if (rc) { destroy_plan(pl); return rc; }
+  *plan = pl;
+  return WG_OK;
+}
+
+int wg_plan_execute(wg_plan* plan, void* stream) {
+  if (!plan) return fail(WG_EINVAL, "plan is NULL");
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  return execute_plan(plan, (cudaStream_t)stream);
+}
+
+int wg_plan_read(wg_plan* plan, double* out, void* stream) {
+  if (!plan || (!out && plan->total_out > 0)) return fail(WG_EINVAL, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (plan->total_out > 0)
+    CK(cudaMemcpyAsync(out, plan->d_out, sizeof(double2) * plan->total_out, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return WG_OK;
+}
+
+int wg_plan_outputs(const wg_plan* plan) { return plan ? plan->total_out : fail(WG_EINVAL, "plan is NULL"); }
+
+int wg_plan_kernel_launches(const wg_plan* plan) {
+  return plan ? (int)plan->groups.size() + (plan->inst.empty() ? 0 : 1) : fail(WG_EINVAL, "plan is NULL");
+}
+
+int wg_plan_destroy(wg_plan* plan) {
+  destroy_plan(plan);
+  return WG_OK;
+}
+
+int wg_run(const wg_instance* inst, int count, int precision, double* out, void* stream) {
+  wg_plan* pl = nullptr;
+  int rc = wg_plan_create(inst, count, precision, 1.0, &pl);
+  if (rc) return rc;
+  rc = wg_plan_execute(pl, stream);
+  if (!rc) rc = wg_plan_read(pl, out, stream);
+  destroy_plan(pl);
+  return rc;
+}
+
+int wg_hafnian(const void* A, int n, int dtype, const int64_t* edge_reps, int E, int glynn, int precision,
+               double out[2], void* stream) {
+  wg_instance in;
+  memset(&in, 0, sizeof(in));
+  in.kind = WG_KIND_PLAIN;
+  in.n = n;
+  in.E = E;
+  in.dtype = dtype;
+  in.glynn = glynn;
+  in.edge_reps = edge_reps;
+  in.A = A;
+  return wg_run(&in, 1, precision, out, stream);
+}
+
+int wg_loop_hafnian(const void* A, const void* D, int n, int dtype, const int64_t* edge_reps, int E, int has_odd,
+                    const double oddloop[2], const void* oddV, int glynn, int precision, double out[2],
+                    void* stream) {
+  wg_instance in;
+  memset(&in, 0, sizeof(in));
+  in.kind = WG_KIND_LOOP;
+  in.n = n;
+  in.E = E;
+  in.dtype = dtype;
+  in.glynn = glynn;
+  in.has_odd = has_odd;
+  in.edge_reps = edge_reps;
+  in.A = A;
+  in.D = D;
+  in.oddV = oddV;
+  if (has_odd && oddloop) { in.oddloop[0] = oddloop[0]; in.oddloop[1] = oddloop[1]; }
+  return wg_run(&in, 1, precision, out, stream);
+}
+
+int wg_loop_hafnian_batch(const void* A, const void* D, int n, int dtype, const int64_t* fixed_edge_reps, int E,
+                          int batch_max, int cutoff, int odd, int glynn, int precision, double* out, void* stream) {
+  wg_instance in;
+  memset(&in, 0, sizeof(in));
+  in.kind = odd ? WG_KIND_BATCH_ODD : WG_KIND_BATCH_EVEN;
+  in.n = n;
+  in.E = E;
+  in.dtype = dtype;
+  in.glynn = glynn;
+  in.batch_max = batch_max;
+  in.cutoff = cutoff;
+  in.edge_reps = fixed_edge_reps;
+  in.A = A;
+  in.D = D;
+  return wg_run(&in, 1, precision, out, stream);
+}
+
+int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops) {
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  if (fp64_tflops) {
+    rc = time_peak<double>(g_num_sms * 4, 256, 2000, fp64_tflops);
+    if (rc) return rc;
+  }
+  if (fp32_tflops) {
+    rc = time_peak<float>(g_num_sms * 8, 256, 20000, fp32_tflops);
+    if (rc) return rc;
+  }
+  return WG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,631 @@
+// Device side of the hafnian / loop-hafnian finite-difference sieve.
+//
+// One warp owns a contiguous range ("chunk") of sieve terms of one instance and walks it in
+// reflected mixed-radix Gray-code order (one edge multiplicity changes by +-1 per step).  For
+// each term it
+//   1. gathers the term matrix AX_S (rows/cols of nonzero delta, columns scaled by delta, halves
+//      swapped) into the warp's shared-memory tile; loop variants border it with D_S / XD_S and
+//      append the odd-mode rows, so that the Krylov data of the loop terms survive the reduction;
+//   2. reduces it to upper Hessenberg form by Gaussian elimination with partial pivoting, with
+//      every subdiagonal entry normalised to exactly 1 (or 0) by a diagonal similarity, so that
+//      La Budde's recurrence needs no subdiagonal products;
+//   3. runs La Budde's recurrence for the first K coefficients of det(I - eta H);
+//   4. forms the term's generating function: det(I - eta H)^(-1/2) (the power-trace
+//      exponential of f / f_loop), times exp of the loop terms for the loop variants;
+//   5. adds prefactor * coefficient into lane-resident Neumaier sums.
+// The reference's per-term pipeline is thewalrus/_hafnian.py:443-462 (plain), :546-569 (loop),
+// thewalrus/loop_hafnian_batch.py:86-116 / :165-201 (batch), with powertrace in
+// thewalrus/charpoly.py:301-327.
+#pragma once
+#include <cstdint>
+
+#include "arith.cuh"
+
+namespace wg {
+
+constexpr int MAX_EDGES = 32;
+constexpr int BINOM_N = 65;
+
+enum Kind : int { KIND_PLAIN = 0, KIND_LOOP = 1, KIND_LOOP_ODD = 2, KIND_BATCH_EVEN = 3, KIND_BATCH_ODD = 4 };
+
+struct InstDev {
+  int kind;
+  int n;          // prepared matrix dimension (2E)
+  int E;          // sieve edges (lanes hold one digit each)
+  int glynn;
+  int N;          // photons (plain / loop); N_fixed for batch kinds
+  int K;          // eta-degree of the plain / even series needed
+  int Nodd;       // zeta-degree of the odd series needed (0 when unused)
+  int nout;       // outputs of this instance (1, or the batch length)
+  int batch_max;
+  int half_first;
+  int unit_binoms;  // every edge multiplicity <= 1: binomial product is 1
+  int nb, ne;       // border rows/cols (0/1) and extra odd-mode rows (0..2)
+  int lda;          // leading dimension of the extended matrix (n + 1)
+  long long a_off;  // byte offset of the extended matrix in the pool
+  long long steps;
+  int radix[MAX_EDGES];
+  int reps[MAX_EDGES];
+  c64 oddloop, oddloop0;
+  // reduction bookkeeping
+  int part_base;   // first partial slot of this instance
+  int nchunks;     // chunks of this instance (partials are [part_base, part_base + nchunks*nout))
+  int out_base;    // first output slot
+  int scale_base;  // first output scale
+};
+
+struct ChunkDev {
+  int inst;
+  int part;  // first partial slot of this chunk
+  long long t0, t1;
+};
+
+// Per-warp shared-memory layout (byte offsets), identical for all warps of one launch.
+struct WarpLayout {
+  int ldw;       // leading dimension of the term tile (odd)
+  int rows;      // tile rows allocated
+  int kw;        // La Budde window size (rows and columns)
+  int nser;      // series capacity (entries per array)
+  int off_x, off_win, off_ser, off_int;
+  int bytes;     // per warp
+};
+
+struct SieveParams {
+  const InstDev* inst;
+  const ChunkDev* chunks;
+  int nchunks;
+  const unsigned char* pool;
+  double2* partials;
+  unsigned int* counter;
+  int* err;
+  WarpLayout L;
+};
+
+__constant__ double c_binom[BINOM_N][BINOM_N];
+__constant__ double c_inv[256];  // c_inv[k] = 1/k (k >= 1)
+
+__device__ __forceinline__ double inv_int(int k) { return k < 256 ? c_inv[k] : 1.0 / (double)k; }
+
+template <class S>
+__device__ __forceinline__ S scale_int(S x, int d) {
+  using A = Ar<S>;
+  if (d == 1) return x;
+  if (d == -1) return A::neg(x);
+  return A::scale(x, (double)d);
+}
+
+template <class S>
+__device__ __forceinline__ S warp_sum(S v) {
+  using A = Ar<S>;
+#pragma unroll
+  for (int off = 16; off; off >>= 1) {
+#pragma unroll
+    for (int c = 0; c < A::NC; ++c) {
+      typename A::Comp x = A::comp(v, c);
+      A::set_comp(v, c, A::cadd(x, A::shfl_xor(x, off)));
+    }
+  }
+  return v;
+}
+
+__device__ __forceinline__ void neumaier(double& s, double& c, double x) {
+  double t = s + x;
+  if (fabs(s) >= fabs(x))
+    c += (s - t) + x;
+  else
+    c += (x - t) + s;
+  s = t;
+}
+
+// ------------------------------------------------------------------------------------------
+// Hessenberg reduction of the warp's tile by Gaussian elimination with partial pivoting.
+// W is rows x ldw (row-major); the square part is mb x mb; rows mb..rows-1 are extra row
+// vectors that receive the column operations only.  After the call W[j+1][j] is exactly 1
+// (or 0 when the column below the diagonal was zero) for j = 0..mb-2.
+template <class S, int NS>
+__device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, int rows, int ldw) {
+  using A = Ar<S>;
+  using Comp = typename A::Comp;
+  const int lane = threadIdx.x & 31;
+  const int r8 = lane & 7, c4 = lane >> 3;
+  constexpr int NCOMP = NS * A::NC;
+  static_assert(NCOMP % 4 == 0, "slot components must split over 4 column lanes");
+
+  for (int j = 0; j + 1 < mb; ++j) {
+    // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1 (ties: lowest row)
+    unsigned long long bk = 0;
+    int bi = j + 1;
+    for (int a = j + 1 + lane; a < mb; a += 32) {
+      unsigned long long k = A::key(W[a * ldw + j]);
+      if (k > bk) { bk = k; bi = a; }
+    }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, off);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+      if (ok > bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
+    }
+    if (bk == 0) {  // nothing to eliminate: subdiagonal entry is an exact zero
+      if (lane == 0) W[(j + 1) * ldw + j] = A::zero();
+      __syncwarp();
+      continue;
+    }
+    const int p = bi;
+    if (p != j + 1) {
+      for (int c = j + lane; c < mb; c += 32) {
+        S t = W[p * ldw + c];
+        W[p * ldw + c] = W[(j + 1) * ldw + c];
+        W[(j + 1) * ldw + c] = t;
+      }
+      __syncwarp();
+      for (int r = lane; r < rows; r += 32) {
+        S t = W[r * ldw + p];
+        W[r * ldw + p] = W[r * ldw + j + 1];
+        W[r * ldw + j + 1] = t;
+      }
+      __syncwarp();
+    }
+    const S piv = W[(j + 1) * ldw + j];
+    const S rp = A::recip(piv);
+    for (int b = j + 1 + lane; b < mb; b += 32) xv[b] = (b == j + 1) ? piv : W[b * ldw + j];
+    __syncwarp();
+    // row j+1 /= piv  (the pivot itself becomes 1)
+    for (int c = j + 1 + lane; c < mb; c += 32) W[(j + 1) * ldw + c] = A::mul(W[(j + 1) * ldw + c], rp);
+    if (lane == 0) W[(j + 1) * ldw + j] = A::one();
+    __syncwarp();
+    // --- phase A: rows j+2..mb-1, cols j+1..mb-1: W[a][b] -= x[a] * W[j+1][b]  (flattened)
+    const int w = mb - j - 1;
+    if (mb - j - 2 > 0) {
+      const int dr = 32 / w, dc = 32 % w;
+      int a = j + 2 + lane / w, b = j + 1 + lane % w;
+      const S* prow = W + (j + 1) * ldw;
+      while (a < mb) {
+        W[a * ldw + b] = A::fnma(xv[a], prow[b], W[a * ldw + b]);
+        b += dc;
+        a += dr;
+        if (b >= mb) { b -= w; a += 1; }
+      }
+    }
+    __syncwarp();
+    // --- phase B: W[a][j+1] = sum_{b=j+1}^{mb-1} W[a][b] x[b] for every row (8 row lanes x 4 col lanes)
+    S acc[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) acc[s] = A::zero();
+    for (int b = j + 1 + c4; b < mb; b += 4) {
+      const S xb = xv[b];
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        const int a = r8 + 8 * s;
+        if (8 * s < rows && a < rows) acc[s] = A::fma(W[a * ldw + b], xb, acc[s]);
+      }
+    }
+    // reduce-scatter across the 4 column lanes (lane bits 3 and 4)
+    Comp v[NCOMP];
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+#pragma unroll
+      for (int c = 0; c < A::NC; ++c) v[s * A::NC + c] = A::comp(acc[s], c);
+    const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
+    Comp u[NCOMP / 2];
+#pragma unroll
+    for (int i = 0; i < NCOMP / 2; ++i) {
+      Comp send = h1 ? v[i] : v[NCOMP / 2 + i];
+      Comp keep = h1 ? v[NCOMP / 2 + i] : v[i];
+      u[i] = A::cadd(keep, A::shfl_xor(send, 16));
+    }
+    Comp z[NCOMP / 4];
+#pragma unroll
+    for (int i = 0; i < NCOMP / 4; ++i) {
+      Comp send = h2 ? u[i] : u[NCOMP / 4 + i];
+      Comp keep = h2 ? u[NCOMP / 4 + i] : u[i];
+      z[i] = A::cadd(keep, A::shfl_xor(send, 8));
+    }
+    __syncwarp();
+    const int base = (h1 ? NCOMP / 2 : 0) + (h2 ? NCOMP / 4 : 0);
+#pragma unroll
+    for (int i = 0; i < NCOMP / 4; ++i) {
+      const int vi = base + i;
+      const int s = vi / A::NC, part = vi % A::NC;
+      const int a = r8 + 8 * s;
+      if (a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// La Budde's recurrence on the unit/zero-subdiagonal Hessenberg block H (block index 1..m maps
+// to tile index nb..nb+m-1).  Writes c[0..Kc] of det(I - eta H) = sum_j c_j eta^j to cpoly.
+//   c[i][j] = c[i-1][j] - H(i,i) c[i-1][j-1] - sum_{r=1}^{j-1} H(i-r,i) c[i-r-1][j-r-1]
+// where the r-sum stops at the last zero subdiagonal entry (charpoly.py:195-282 with all
+// subdiagonal products equal to 1).
+template <class S>
+__device__ void labudde(const S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __restrict__ win, int kw,
+                        S* __restrict__ cpoly) {
+  using A = Ar<S>;
+  const int lane = threadIdx.x & 31;
+  for (int jj = lane; jj <= Kc; jj += 32) win[jj] = (jj == 0) ? A::one() : A::zero();
+  __syncwarp();
+  int zlast = 1;
+  int prow = 0;  // window slot of row i-1
+  for (int i = 1; i <= m; ++i) {
+    const int wi = nb + i - 1;
+    if (i >= 2 && A::is_zero(W[wi * ldw + wi - 1])) zlast = i;
+    const int rmax = i - zlast;
+    const S alpha = W[wi * ldw + wi];
+    const int Ki = i < Kc ? i : Kc;
+    const int crow = prow + 1 == kw ? 0 : prow + 1;
+    for (int jj = lane + 1; jj <= Ki; jj += 32) {
+      S val = (jj <= i - 1) ? win[prow * kw + jj] : A::zero();
+      val = A::fnma(alpha, win[prow * kw + jj - 1], val);
+      const int rlim = (jj - 1) < rmax ? (jj - 1) : rmax;
+      int slot = prow;  // slot of row i-r-1 for r = 1 is prow - 1
+      for (int r = 1; r <= rlim; ++r) {
+        slot = slot == 0 ? kw - 1 : slot - 1;
+        val = A::fnma(W[(wi - r) * ldw + wi], win[slot * kw + (jj - r - 1)], val);
+      }
+      win[crow * kw + jj] = val;
+    }
+    if (lane == 0) win[crow * kw] = A::one();
+    prow = crow;
+    __syncwarp();
+  }
+  for (int jj = lane; jj <= Kc; jj += 32) cpoly[jj] = win[prow * kw + jj];
+  __syncwarp();
+}
+
+// g = (sum_j c_j eta^j)^(-1/2) up to degree G:  n g_n = -sum_{i=1}^{n} c_i (n - i/2) g_{n-i}
+template <class S>
+__device__ void inv_sqrt_series(const S* __restrict__ cpoly, int Kc, S* __restrict__ g, int G) {
+  using A = Ar<S>;
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) g[0] = A::one();
+  __syncwarp();
+  for (int nn = 1; nn <= G; ++nn) {
+    const int lim = nn < Kc ? nn : Kc;
+    S part = A::zero();
+    for (int i = lane + 1; i <= lim; i += 32)
+      part = A::fma(A::scale(cpoly[i], (double)nn - 0.5 * (double)i), g[nn - i], part);
+    part = warp_sum(part);
+    if (lane == 0) g[nn] = A::scale(part, -inv_int(nn));
+    __syncwarp();
+  }
+}
+
+// e = exp(sum_{l=1}^{Q} q_l z^l) up to degree G:  n e_n = sum_{l=1}^{n} l q_l e_{n-l}
+template <class S>
+__device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, int G) {
+  using A = Ar<S>;
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) e[0] = A::one();
+  __syncwarp();
+  for (int nn = 1; nn <= G; ++nn) {
+    const int lim = nn < Q ? nn : Q;
+    S part = A::zero();
+    for (int l = lane + 1; l <= lim; l += 32) part = A::fma(A::scale(q[l], (double)l), e[nn - l], part);
+    part = warp_sum(part);
+    if (lane == 0) e[nn] = A::scale(part, inv_int(nn));
+    __syncwarp();
+  }
+}
+
+// Warp-cooperative Krylov data of the loop variants, on the reduced tile.
+// v_1 = e_1, v_{t+1} = H v_t (H the m x m block).  For t = 1..T:
+//   lam[t] = d * x.v_t  (x = tile row 0, cols 1..m),  mu[t] = d * y.v_t (tile row mb), mu0 likewise.
+template <class S>
+__device__ void loop_krylov(const S* __restrict__ W, int ldw, int m, int mb, int ne, int T, S* __restrict__ v,
+                            S* __restrict__ vn, S* __restrict__ lam, S* __restrict__ mu, S* __restrict__ mu0) {
+  using A = Ar<S>;
+  const int lane = threadIdx.x & 31;
+  const bool dnz = !A::is_zero(W[1 * ldw + 0]);
+  if (!dnz || m == 0) {
+    for (int t = lane; t <= T; t += 32) {
+      lam[t] = A::zero();
+      if (ne > 0) mu[t] = A::zero();
+      if (ne > 1) mu0[t] = A::zero();
+    }
+    __syncwarp();
+    return;
+  }
+  const S d = W[1 * ldw + 0];
+  for (int s = lane; s <= m; s += 32) v[s] = (s == 1) ? A::one() : A::zero();
+  __syncwarp();
+  for (int t = 1; t <= T; ++t) {
+    const int sup = t < m ? t : m;  // support of v_t: block indices 1..sup
+    S pl = A::zero(), pm = A::zero(), p0 = A::zero();
+    for (int s = lane + 1; s <= sup; s += 32) {
+      pl = A::fma(W[0 * ldw + s], v[s], pl);
+      if (ne > 0) pm = A::fma(W[mb * ldw + s], v[s], pm);
+      if (ne > 1) p0 = A::fma(W[(mb + 1) * ldw + s], v[s], p0);
+    }
+    pl = warp_sum(pl);
+    if (ne > 0) pm = warp_sum(pm);
+    if (ne > 1) p0 = warp_sum(p0);
+    if (lane == 0) {
+      lam[t] = A::mul(d, pl);
+      if (ne > 0) mu[t] = A::mul(d, pm);
+      if (ne > 1) mu0[t] = A::mul(d, p0);
+    }
+    if (t == T) break;
+    const int nsup = (t + 1) < m ? (t + 1) : m;
+    for (int rho = lane + 1; rho <= nsup; rho += 32) {
+      S acc = A::zero();
+      const int s0 = rho > 1 ? rho - 1 : 1;
+      for (int s = s0; s <= sup; ++s) acc = A::fma(W[rho * ldw + s], v[s], acc);
+      vn[rho] = acc;
+    }
+    __syncwarp();
+    for (int rho = lane + 1; rho <= nsup; rho += 32) v[rho] = vn[rho];
+    __syncwarp();
+  }
+  __syncwarp();
+}
+
+// ------------------------------------------------------------------------------------------
+template <class S, int NS>
+__global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
+  using A = Ar<S>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const WarpLayout& L = P.L;
+  unsigned char* ws = smem + (size_t)warp * L.bytes;
+  S* W = reinterpret_cast<S*>(ws);
+  S* xv = reinterpret_cast<S*>(ws + L.off_x);
+  S* win = reinterpret_cast<S*>(ws + L.off_win);
+  S* ser = reinterpret_cast<S*>(ws + L.off_ser);
+  int* srow = reinterpret_cast<int*>(ws + L.off_int);
+  int* scol = srow + L.rows;
+  int* sdel = scol + L.ldw;
+  const int ldw = L.ldw;
+  const int ns = L.nser;
+  S* cpoly = ser;           // [0, ns)
+  S* gser = ser + ns;       // [ns, 2ns)
+  S* eser = ser + 2 * ns;   // even exp series / Krylov scratch
+  S* oser = ser + 3 * ns;   // odd exp series
+  S* lam = ser + 4 * ns;
+  S* mu = ser + 5 * ns;
+  S* mu0 = ser + 6 * ns;
+  S* qv = ser + 7 * ns;     // series exponents
+
+  for (;;) {
+    int c = 0;
+    if (lane == 0) c = (int)atomicAdd(P.counter, 1u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if (c >= P.nchunks) break;
+    const ChunkDev ch = P.chunks[c];
+    const InstDev& I = P.inst[ch.inst];
+    const int kind = I.kind, E = I.E, n = I.n, nb = I.nb, ne = I.ne, glynn = I.glynn;
+    const int lda = I.lda;
+    const S* Aext = reinterpret_cast<const S*>(P.pool + I.a_off);
+    const int R = lane < E ? I.radix[lane] : 1;
+    const int rep = lane < E ? I.reps[lane] : 0;
+    const int nout = I.nout;
+
+    // initial reflected mixed-radix Gray digits of t0 (edge 0 most significant)
+    int myd = 0;
+    {
+      long long tt = ch.t0;
+      for (int i = E - 1; i >= 0; --i) {
+        const int Ri = I.radix[i];
+        const int d = (int)(tt % Ri);
+        tt /= Ri;
+        if (lane == i) myd = d;
+      }
+    }
+    int g = 0, dir = 1;
+    {
+      int f = 0;
+      for (int i = 0; i < E; ++i) {
+        const int d = __shfl_sync(0xffffffffu, myd, i);
+        const int Ri = I.radix[i];
+        const int gi = f ? Ri - 1 - d : d;
+        if (lane == i) { g = gi; dir = f ? -1 : 1; }
+        f ^= (gi & 1);
+      }
+    }
+    double s_re = 0, s_im = 0, k_re = 0, k_im = 0;  // lane o: Neumaier sum of output o
+
+    for (long long t = ch.t0; t < ch.t1; ++t) {
+      if (t != ch.t0) {  // Gray step: least significant digit that can move in its direction
+        const int ng = g + dir;
+        const unsigned can = __ballot_sync(0xffffffffu, lane < E && ng >= 0 && ng < R);
+        const int i = 31 - __clz(can);
+        if (lane == i) g = ng;
+        if (lane > i && lane < E) dir = -dir;
+      }
+      const int delta = lane < E ? (glynn ? 2 * g - rep : g) : 0;
+      const unsigned nz = __ballot_sync(0xffffffffu, delta != 0);
+      const int Ep = __popc(nz);
+      const int m = 2 * Ep;
+      const int mb = m + nb;
+      const int rows = mb + ne;
+      // kept-sum and binomial product
+      int ksum = lane < E ? g : 0;
+#pragma unroll
+      for (int off = 16; off; off >>= 1) ksum += __shfl_xor_sync(0xffffffffu, ksum, off);
+      const bool batch = kind >= KIND_BATCH_EVEN;
+      double bin = 1.0;
+      if (!I.unit_binoms) {
+        bin = (lane < E && !(batch && lane == 0)) ? c_binom[rep][g] : 1.0;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) bin *= __shfl_xor_sync(0xffffffffu, bin, off);
+      }
+      const int g0 = __shfl_sync(0xffffffffu, g, 0);
+      const int g1 = __shfl_sync(0xffffffffu, g, 1);
+      const int d0 = __shfl_sync(0xffffffffu, delta, 0);
+      // index maps of the tile
+      if (delta != 0) {
+        const int pos = __popc(nz & ((1u << lane) - 1u));
+        srow[nb + pos] = lane;
+        srow[nb + Ep + pos] = E + lane;
+        scol[nb + pos] = E + lane;
+        scol[nb + Ep + pos] = lane;
+        sdel[nb + pos] = delta;
+        sdel[nb + Ep + pos] = delta;
+      }
+      if (lane == 0 && nb) { srow[0] = n; scol[0] = n; sdel[0] = 1; }
+      if (lane < ne) srow[mb + lane] = n + 1 + lane;
+      __syncwarp();
+      // gather the tile
+      if (mb > 0) {
+        const int total = rows * mb;
+        const int dr = 32 / mb, dc = 32 % mb;
+        int r = lane / mb, cc = lane % mb;
+        for (int e = lane; e < total; e += 32) {
+          const S x = Aext[(size_t)srow[r] * lda + scol[cc]];
+          W[r * ldw + cc] = scale_int(x, sdel[cc]);
+          cc += dc;
+          r += dr;
+          if (cc >= mb) { cc -= mb; r += 1; }
+        }
+      }
+      __syncwarp();
+      hessenberg_elim<S, NS>(W, xv, mb, rows, ldw);
+      // characteristic polynomial coefficients of the block
+      const int Kc = I.K < m ? I.K : m;
+      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, cpoly);
+      const int Gdeg = I.K;  // degree of det^(-1/2) needed
+      inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
+
+      if (kind == KIND_PLAIN) {
+        if (lane == 0) {
+          double pre = ((I.N / 2 - ksum) & 1) ? -bin : bin;
+          if (glynn && d0 == 0) pre *= 0.5;
+          const c64 f = A::to_c64(gser[I.K]);
+          neumaier(s_re, k_re, pre * f.re);
+          neumaier(s_im, k_im, pre * f.im);
+        }
+      } else {
+        const int T = I.K;
+        loop_krylov<S>(W, ldw, m, mb, ne, T, xv, eser, lam, mu, mu0);  // xv is free after the reduction
+        // even series: q_l = lam_l / 2, e = exp(q), f_even[h] = sum_t g_t e_{h-t}
+        if (kind == KIND_LOOP || kind == KIND_BATCH_EVEN || kind == KIND_BATCH_ODD) {
+          for (int l = lane; l <= T; l += 32) qv[l] = l ? A::scale(lam[l], 0.5) : A::zero();
+          __syncwarp();
+          exp_series<S>(qv, T, eser, T);
+        }
+        if (kind == KIND_LOOP) {
+          S part = A::zero();
+          for (int tq = lane; tq <= T; tq += 32) part = A::fma(gser[tq], eser[T - tq], part);
+          part = warp_sum(part);
+          if (lane == 0) {
+            double pre = ((I.N / 2 - ksum) & 1) ? -bin : bin;
+            if (glynn && d0 == 0) pre *= 0.5;
+            const c64 f = A::to_c64(part);
+            neumaier(s_re, k_re, pre * f.re);
+            neumaier(s_im, k_im, pre * f.im);
+          }
+        } else {
+          // odd series in zeta: q'_1 = oddloop, q'_{2l} = lam_l/2, q'_{2l+1} = mu_l
+          const int No = I.Nodd;
+          __syncwarp();
+          for (int l = lane; l <= No; l += 32) {
+            S q;
+            if (l == 0) q = A::zero();
+            else if (l == 1) q = A::from_c64(I.oddloop);
+            else if ((l & 1) == 0) q = (l / 2 <= T) ? A::scale(lam[l / 2], 0.5) : A::zero();
+            else q = ((l - 1) / 2 <= T) ? mu[(l - 1) / 2] : A::zero();
+            qv[l] = q;
+          }
+          __syncwarp();
+          exp_series<S>(qv, No, oser, No);
+          if (kind == KIND_LOOP_ODD) {
+            S part = A::zero();
+            for (int tq = lane; 2 * tq <= No; tq += 32) part = A::fma(gser[tq], oser[No - 2 * tq], part);
+            part = warp_sum(part);
+            if (lane == 0) {
+              const double pre = ((I.N / 2 - ksum) & 1) ? -bin : bin;
+              const c64 f = A::to_c64(part);
+              neumaier(s_re, k_re, pre * f.re);
+              neumaier(s_im, k_im, pre * f.im);
+            }
+          } else {
+            // batch: lane o handles output N_det = o
+            const bool odd = kind == KIND_BATCH_ODD;
+            const int Nf = I.N;
+            if (odd && g0 == 0 && g1 == 0) {
+              // f_loop_odd at N_fixed with the second odd mode (loop_hafnian_batch.py:181-185)
+              __syncwarp();
+              for (int l = lane; l <= Nf; l += 32) {
+                S q;
+                if (l == 0) q = A::zero();
+                else if (l == 1) q = A::from_c64(I.oddloop0);
+                else if ((l & 1) == 0) q = (l / 2 <= T) ? A::scale(lam[l / 2], 0.5) : A::zero();
+                else q = ((l - 1) / 2 <= T) ? mu0[(l - 1) / 2] : A::zero();
+                qv[l] = q;
+              }
+              __syncwarp();
+              exp_series<S>(qv, Nf, mu0, Nf);  // mu0 was copied into qv above
+              S part = A::zero();
+              for (int tq = lane; 2 * tq <= Nf; tq += 32) part = A::fma(gser[tq], mu0[Nf - 2 * tq], part);
+              part = warp_sum(part);
+              if (lane == 0) {
+                const double pre = ((Nf / 2 - ksum) & 1) ? -bin : bin;
+                const c64 f = A::to_c64(part);
+                neumaier(s_re, k_re, pre * f.re);
+                neumaier(s_im, k_im, pre * f.im);
+              }
+            }
+            __syncwarp();
+            for (int o = 0; o < nout; ++o) {
+              const int start = odd ? 2 * g0 + 1 : 2 * g0;
+              if (o < start) continue;
+              const int Nn = Nf + o;
+              S part = A::zero();
+              if ((Nn & 1) == 0) {
+                const int h = Nn / 2;
+                for (int tq = lane; tq <= h; tq += 32) part = A::fma(gser[tq], eser[h - tq], part);
+              } else {
+                for (int tq = lane; 2 * tq <= Nn; tq += 32) part = A::fma(gser[tq], oser[Nn - 2 * tq], part);
+              }
+              part = warp_sum(part);
+              if (lane == o % 32) {
+                const int bi = odd ? (o - 1) / 2 : o / 2;
+                double pre = c_binom[bi][g0] * bin;
+                if ((Nn / 2 - ksum) & 1) pre = -pre;
+                const c64 f = A::to_c64(part);
+                neumaier(s_re, k_re, pre * f.re);
+                neumaier(s_im, k_im, pre * f.im);
+              }
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (lane < nout) P.partials[ch.part + lane] = make_double2(s_re + k_re, s_im + k_im);
+    __syncwarp();
+  }
+}
+
+// One thread per output: Neumaier sum of the instance's chunk partials in chunk order, then the
+// final scale (0.5^(N/2-1) etc., and the undoing of any input prescaling).  The last thread
+// re-arms the work counters for the next execution.
+__global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst, const double2* __restrict__ partials,
+                              const double* __restrict__ scales, double2* __restrict__ out, unsigned int* counters,
+                              int ncounters, int total_out) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid < total_out) {
+    // locate the instance (outputs are laid out instance by instance)
+    int lo = 0, hi = ninst - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (inst[mid].out_base <= tid) lo = mid; else hi = mid - 1;
+    }
+    const InstDev& I = inst[lo];
+    const int o = tid - I.out_base;
+    double sr = 0, si = 0, cr = 0, ci = 0;
+    for (int c = 0; c < I.nchunks; ++c) {
+      const double2 v = partials[I.part_base + c * I.nout + o];
+      neumaier(sr, cr, v.x);
+      neumaier(si, ci, v.y);
+    }
+    const double sc = scales[I.scale_base + o];
+    out[tid] = make_double2((sr + cr) * sc, (si + ci) * sc);
+  }
+  if (tid == 0)
+    for (int i = 0; i < ncounters; ++i) counters[i] = 0u;
+}
+
+}  // namespace wg
