@@ -1,0 +1,289 @@
+"""Benchmark: n=40 hafnians/s on one GB300 (or N GPUs as independent shards).
+
+Workload: the plain Glynn hafnian of a 40x40 complex128 symmetric matrix A = (G + G^T)/2,
+Re G, Im G ~ N(0, 1/2) iid, seed 0 (524,288 sieve terms).  One step = one hafnian.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|df] [--impl gb300|reference]
+
+value    : hafnians/s with the input resident in HBM (device time of the sieve + reduction
+           launches, CUDA events on the launching stream, L2 flushed between steps), summed
+           over ranks (each rank runs its own shard of hafnians: weak scaling).
+e2e      : the same metric through the public API thewalrus_gb300.hafnian(A) from host NumPy
+           input: host preparation, host->device upload, kernels, device->host result.
+roofline : algorithmic flops of the sieve (thewalrus_gb300.costmodel) / mean device time,
+           against the FP64 (or, for df, FP32) FMA-pipe peak measured in the same run.
+cpu_baseline : the CPU oracle (a C restatement of the reference algorithm: mixed-radix term
+           order, power traces by repeated matrix products) on all host cores, timed on a
+           bounded sample of the same hafnian's terms and scaled to hafnians/s.
+--impl reference : that CPU restatement alone, as the reference arm (rank 0 only).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_MATRIX = 40
+METRIC = "n=40 hafnians/s (complex128, Glynn sieve)"
+UNIT = "hafnians/s"
+
+
+def workload(n=N_MATRIX):
+    from thewalrus_gb300 import workloads as wl
+
+    return wl.complex_symmetric(n, seed=0)
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_sample(seconds=12.0, threads=None):
+    """Time the CPU oracle on terms [0, S) of the n=40 sieve; returns (hafnians/s, info)."""
+    import numpy as np
+
+    import oracle
+
+    threads = threads or os.cpu_count() or 1
+    A = workload()
+    x, reps, _ = oracle.matched_reps([1] * N_MATRIX)
+    Ax = A[np.ix_(x, x)]
+    total_terms = 2 ** (N_MATRIX // 2 - 1)
+    probe = 4 * threads
+    t0 = time.perf_counter()
+    oracle.haf_term_range(Ax, reps, 0, probe, nthreads=threads)
+    dt = time.perf_counter() - t0
+    S = int(min(total_terms, max(probe, probe * seconds / max(dt, 1e-6))))
+    t0 = time.perf_counter()
+    oracle.haf_term_range(Ax, reps, 0, S, nthreads=threads)
+    dt = time.perf_counter() - t0
+    rate = S / dt / total_terms
+    info = {"terms": S, "seconds": dt, "threads": threads, "total_terms": total_terms}
+    return rate, info
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sms, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sms.append(float(parts[1]))
+                    maxes.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if sms:
+            out = {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxes),
+                   "reasons": sorted(reasons), "samples": len(sms)}
+        return out
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rates = []
+    info = None
+    per_step = float(os.environ.get("BENCH_REF_STEP_SECONDS", "6"))
+    for i in range(args.warmup + args.steps):
+        r, info = cpu_sample(seconds=per_step, threads=threads)
+        if i >= args.warmup:
+            rates.append(r)
+    value = statistics.mean(rates)
+    sample = ("terms [0, %d) of the %d-term n=40 sieve per step, C restatement of the reference "
+              "algorithm (double, %d threads), scaled to whole hafnians" %
+              (info["terms"], info["total_terms"], threads))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic", "config": {"workload": "hafnian 40x40 complex128, seed 0"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    import thewalrus_gb300 as tw
+    from thewalrus_gb300 import _native as nat
+    from thewalrus_gb300 import costmodel
+
+    nat.check(nat.load().wg_init(local))
+    n = args.n
+    A = workload(n)
+    inst = tw.prepare_hafnian(A)
+    plan = nat.Plan([inst], precision=args.precision)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    fp64_peak, fp32_peak = nat.measure_fp_peaks()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")
+    for _ in range(args.warmup):
+        plan.execute(sptr)
+    torch.cuda.synchronize()
+    result = plan.read(sptr)[0]
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for e0, e1 in evs:
+        flush.zero_()
+        e0.record(stream)
+        plan.execute(sptr)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clk = clocks.stop()
+    step_ms = [e0.elapsed_time(e1) for e0, e1 in evs]
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps / (total_ms * 1e-3)
+
+    # end to end through the public API: host prep + upload + kernels + result download
+    for _ in range(min(args.warmup, 2)):
+        tw.hafnian(A, precision=args.precision)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r = tw.hafnian(A, precision=args.precision)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps / e2e_s
+    h2d, d2h = plan.transfer_bytes()
+
+    flops = costmodel.plain_hafnian_flops(n, complex_input=True)
+    mean_s = total_ms / args.steps * 1e-3
+    achieved = flops / mean_s / 1e12
+    peak = fp64_peak if args.precision == "fp64" else fp32_peak
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "sieve_c64_n40_traffic.json")
+    if os.path.exists(prof):
+        try:
+            traffic = json.load(open(prof)).get("bytes_per_launch")
+        except (OSError, ValueError):
+            traffic = None
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "df32",
+        "data": "synthetic",
+        "config": {"workload": "hafnian %dx%d complex128 (G+G^T)/2, seed 0, %d sieve terms"
+                               % (n, n, 2 ** (n // 2 - 1)),
+                   "precision": args.precision, "parallelism": "shard-per-gpu" if world > 1 else "1 gpu",
+                   "l2": "flushed between steps (256 MiB write, outside the timed events)"},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": "FMA-pipe microbenchmark (wg_measure_fp_peaks) in this run",
+                     "flops_per_launch": flops},
+        "gpu_launches": args.steps * plan.kernel_launches,
+        "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
+        "result": [float(np.real(result)), float(np.imag(result))],
+        "e2e_result_matches": bool(abs(r - result) <= 1e-12 * abs(result)),
+    }
+    if n != N_MATRIX:
+        line["metric"] = "n=%d hafnians/s (complex128, Glynn sieve)" % n
+    if not args.no_cpu_baseline and n == N_MATRIX:
+        rate, info = cpu_sample(seconds=args.cpu_seconds)
+        line["cpu_baseline"] = {
+            "value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
+            "sample": "terms [0, %d) of the %d-term sieve in %.1f s, C restatement of the reference "
+                      "algorithm in double on %d threads" % (info["terms"], info["total_terms"],
+                                                             info["seconds"], info["threads"])}
+    print(json.dumps(line), flush=True)
+    plan.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--n", type=int, default=N_MATRIX, help="matrix size (40 is the benchmark)")
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--precision", choices=["fp64", "df"], default="fp64")
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -95,6 +95,14 @@ int wg_plan_execute(wg_plan* plan, void* stream);
 int wg_plan_read(wg_plan* plan, double* out, void* stream);
 int wg_plan_outputs(const wg_plan* plan);
 int wg_plan_kernel_launches(const wg_plan* plan);
+/* Diagnostics for chunk-level checks.  wg_plan_partials copies the unscaled per-chunk partial
+ * sums (complex interleaved, nout per chunk) of the last execution when capacity (in complex
+ * values) suffices and returns their count.  wg_plan_chunk describes chunk `chunk`: its
+ * instance, first partial slot and Gray-code term range [t0, t1); returns the chunk count. */
+int wg_plan_partials(wg_plan* plan, double* out, int capacity, void* stream);
+int wg_plan_chunk(const wg_plan* plan, int chunk, int* inst, int* part, long long* t0, long long* t1);
+/* Bytes moved by wg_plan_create (host to device) and by wg_plan_read (device to host). */
+int wg_plan_transfer_bytes(const wg_plan* plan, long long* h2d, long long* d2h);
 int wg_plan_destroy(wg_plan* plan);
 /* create + execute + read + destroy */
 int wg_run(const wg_instance* inst, int count, int precision, double* out, void* stream);

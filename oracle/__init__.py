@@ -31,6 +31,7 @@ __all__ = [
     "loop_hafnian",
     "loop_hafnian_batch",
     "haf_prepared",
+    "haf_term_range",
     "loop_haf_prepared",
     "powertrace",
     "charpoly",
@@ -58,6 +59,9 @@ def _load():
             f = getattr(lib, "oracle_calc_loop_hafnian_batch" + sfx)
             f.argtypes = [dp, dp, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                           ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
+            f = getattr(lib, "oracle_hafnian_term_range" + sfx)
+            f.argtypes = [dp, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                          ctypes.c_int64, ctypes.c_int64, dp]
             f = getattr(lib, "oracle_powertrace" + sfx)
             f.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
             f = getattr(lib, "oracle_charpoly" + sfx)
@@ -141,6 +145,19 @@ def haf_prepared(Ax, edge_reps, glynn=True, precision="double", nthreads=None):
     getattr(lib, "oracle_calc_hafnian" + _SFX[precision])(
         pA, A.shape[0], pr, len(r), int(bool(glynn)), nthreads or _default_threads(),
         out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return DD(*_dd(out))
+
+
+def haf_term_range(Ax, edge_reps, t_begin, t_end, glynn=True, precision="double", nthreads=None):
+    """Unscaled sum of the plain sieve's terms [t_begin, t_end) on prepared inputs, in the
+    reference's mixed-radix term order: a bounded sample of one hafnian's CPU work."""
+    lib = _load()
+    A, pA = _cbuf(Ax)
+    r, pr = _ibuf(edge_reps)
+    out = np.zeros(4)
+    getattr(lib, "oracle_hafnian_term_range" + _SFX[precision])(
+        pA, A.shape[0], pr, len(r), int(bool(glynn)), nthreads or _default_threads(),
+        int(t_begin), int(t_end), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     return DD(*_dd(out))
 
 

@@ -409,12 +409,15 @@ static void FN(store_dd)(C v, double* out) {
 /* The sum over sieve terms.  Each thread sums a contiguous range; the thread partials are then
  * added in thread order.  `kind`: 0 plain, 1 loop (even), 2 loop with odd self-loop. */
 static C FN(sieve)(int kind, const C* A, const C* D, int n, const int64_t* reps, int E, C oddloop,
-                   const C* oddV, int glynn, int nthreads) {
+                   const C* oddV, int glynn, int nthreads, int64_t t_begin, int64_t t_end, int scale) {
   int N = 0;
   for (int i = 0; i < E; ++i) N += 2 * (int)reps[i];
   if (kind == 2) N += 1;
   int half_first = glynn && kind != 2;
   int64_t steps = FN(prod_radix)(reps, E, half_first);
+  if (t_end < 0 || t_end > steps) t_end = steps;
+  if (t_begin < 0) t_begin = 0;
+  int64_t span = t_end > t_begin ? t_end - t_begin : 0;
   int64_t maxrep = 0;
   for (int i = 0; i < E; ++i) maxrep = reps[i] > maxrep ? reps[i] : maxrep;
   int mb = (int)maxrep + 1;
@@ -428,7 +431,7 @@ static C FN(sieve)(int kind, const C* A, const C* D, int n, const int64_t* reps,
     tid = omp_get_thread_num();
     nt = omp_get_num_threads();
 #endif
-    int64_t lo = steps * tid / nt, hi = steps * (tid + 1) / nt;
+    int64_t lo = t_begin + span * tid / nt, hi = t_begin + span * (tid + 1) / nt;
     int mm = n > 0 ? n : 1;
     FN(ws_t) w;
     FN(ws_init)(&w, mm);
@@ -478,7 +481,7 @@ static C FN(sieve)(int kind, const C* A, const C* D, int n, const int64_t* reps,
   for (int t = 0; t < nthreads; ++t) H = FN(cadd)(H, partial[t]);
   free(partial);
   free(binoms);
-  if (glynn) {
+  if (glynn && scale) {
     int e = (kind == 2) ? N / 2 : N / 2 - 1;
     R s = 1;
     for (int i = 0; i < e; ++i) s *= (R)0.5;
@@ -494,7 +497,18 @@ int FN(oracle_calc_hafnian)(const double* A, int n, const int64_t* edge_reps, in
                             int nthreads, double* out) {
   C* Ac = (C*)malloc(sizeof(C) * (n > 0 ? n * n : 1));
   FN(load_c)(A, Ac, (size_t)n * n);
-  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads);
+  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads, 0, -1, 1);
+  FN(store_dd)(h, out);
+  free(Ac);
+  return 0;
+}
+
+/* Unscaled partial sum of the plain sieve over terms [t_begin, t_end) (bounded CPU samples). */
+int FN(oracle_hafnian_term_range)(const double* A, int n, const int64_t* edge_reps, int E, int glynn,
+                                  int nthreads, int64_t t_begin, int64_t t_end, double* out) {
+  C* Ac = (C*)malloc(sizeof(C) * (n > 0 ? n * n : 1));
+  FN(load_c)(A, Ac, (size_t)n * n);
+  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads, t_begin, t_end, 0);
   FN(store_dd)(h, out);
   free(Ac);
   return 0;
@@ -513,7 +527,7 @@ int FN(oracle_calc_loop_hafnian)(const double* A, const double* D, int n, const 
     FN(load_c)(oddV, Vc, (size_t)n);
     ol = FN(cmk)((R)oddloop[0], (R)oddloop[1]);
   }
-  C h = FN(sieve)(has_odd ? 2 : 1, Ac, Dc, n, edge_reps, E, ol, has_odd ? Vc : NULL, glynn, nthreads);
+  C h = FN(sieve)(has_odd ? 2 : 1, Ac, Dc, n, edge_reps, E, ol, has_odd ? Vc : NULL, glynn, nthreads, 0, -1, 1);
   FN(store_dd)(h, out);
   free(Ac); free(Dc); free(Vc);
   return 0;

@@ -84,7 +84,9 @@ class WgInstance(ctypes.Structure):
 EXPORTS = [
     "wg_init", "wg_last_error", "wg_instance_outputs", "wg_hafnian", "wg_loop_hafnian",
     "wg_loop_hafnian_batch", "wg_plan_create", "wg_plan_execute", "wg_plan_read", "wg_plan_outputs",
-    "wg_plan_kernel_launches", "wg_plan_destroy", "wg_run", "wg_measure_fp_peaks",
+    "wg_plan_kernel_launches", "wg_plan_partials", "wg_plan_chunk", "wg_plan_transfer_bytes",
+    "wg_plan_destroy", "wg_run",
+    "wg_measure_fp_peaks",
 ]
 
 
@@ -112,6 +114,10 @@ def load(build_if_needed=True):
     lib.wg_plan_read.argtypes = [vp, dp, vp]
     lib.wg_plan_outputs.argtypes = [vp]
     lib.wg_plan_kernel_launches.argtypes = [vp]
+    lib.wg_plan_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
+    lib.wg_plan_partials.argtypes = [vp, dp, i32, vp]
+    lib.wg_plan_chunk.argtypes = [vp, i32, ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                  ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
     lib.wg_plan_destroy.argtypes = [vp]
     lib.wg_run.argtypes = [ctypes.POINTER(WgInstance), i32, i32, dp, vp]
     lib.wg_measure_fp_peaks.argtypes = [dp, dp]
@@ -182,6 +188,31 @@ class Plan:
         self.handle = h
         self.total_out = self.lib.wg_plan_outputs(h)
         self.kernel_launches = self.lib.wg_plan_kernel_launches(h)
+
+    def transfer_bytes(self):
+        h, d = ctypes.c_longlong(), ctypes.c_longlong()
+        check(self.lib.wg_plan_transfer_bytes(self.handle, ctypes.byref(h), ctypes.byref(d)))
+        return h.value, d.value
+
+    def partials(self, stream=0):
+        """Unscaled per-chunk partial sums of the last execution, with each chunk's
+        (instance, first slot, t0, t1)."""
+        cnt = self.lib.wg_plan_partials(self.handle, None, 0, ctypes.c_void_p(stream))
+        out = np.zeros(2 * max(cnt, 1))
+        self.lib.wg_plan_partials(self.handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                  cnt, ctypes.c_void_p(stream))
+        chunks = []
+        a, b = ctypes.c_int(), ctypes.c_int()
+        t0, t1 = ctypes.c_longlong(), ctypes.c_longlong()
+        k = 0
+        while True:
+            n = self.lib.wg_plan_chunk(self.handle, k, ctypes.byref(a), ctypes.byref(b),
+                                       ctypes.byref(t0), ctypes.byref(t1))
+            if n <= k:
+                break
+            chunks.append((a.value, b.value, t0.value, t1.value))
+            k += 1
+        return (out[0::2] + 1j * out[1::2])[:cnt], chunks
 
     def execute(self, stream=0):
         check(self.lib.wg_plan_execute(self.handle, ctypes.c_void_p(stream)))

@@ -26,6 +26,61 @@ namespace wg {
 static thread_local std::string g_err;
 static int g_device = -1;
 static int g_num_sms = 0;
+static LbLane* g_lb_lane = nullptr;
+static LbOwner* g_lb_own = nullptr;
+
+// Balanced La Budde schedule for triangle size Ki: coefficient j (2..Ki) needs j-1 products.
+// Find the smallest per-lane load t for which the pieces (each j's products cut into
+// ceil((j-1)/t) near-equal runs) pack into 32 lanes with at most two pieces per lane
+// (largest piece first, onto the least-loaded lane that fits).
+static bool lb_schedule(int Ki, LbLane* lanes, LbOwner* own) {
+  for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
+  const int W = Ki * (Ki - 1) / 2;
+  if (W == 0) return true;
+  struct Piece { int j, rlo, len; };
+  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
+    std::vector<Piece> pcs;
+    for (int j = 2; j <= Ki; ++j) {
+      const int x = j - 1, p = (x + t - 1) / t;
+      int r = 1;
+      for (int q = 0; q < p; ++q) {
+        const int len = x / p + (q < x % p ? 1 : 0);
+        pcs.push_back({j, r, len});
+        r += len;
+      }
+    }
+    if ((int)pcs.size() > 64) continue;
+    std::stable_sort(pcs.begin(), pcs.end(), [](const Piece& a, const Piece& b) { return a.len > b.len; });
+    int load[32] = {0}, nseg[32] = {0};
+    Piece seg[32][2];
+    bool ok = true;
+    for (const Piece& pc : pcs) {
+      int best = -1;
+      for (int l = 0; l < 32; ++l)
+        if (nseg[l] < 2 && load[l] + pc.len <= t && (best < 0 || load[l] < load[best])) best = l;
+      if (best < 0) { ok = false; break; }
+      seg[best][nseg[best]++] = pc;
+      load[best] += pc.len;
+    }
+    if (!ok) continue;
+    bool fits = true;
+    for (int l = 0; l < 32 && fits; ++l) {
+      LbLane& L = lanes[l];
+      if (nseg[l] > 0) { L.ja = (signed char)seg[l][0].j; L.rloa = (signed char)seg[l][0].rlo; L.lena = (signed char)seg[l][0].len; }
+      if (nseg[l] > 1) { L.jb = (signed char)seg[l][1].j; L.rlob = (signed char)seg[l][1].rlo; L.lenb = (signed char)seg[l][1].len; }
+      for (int k = 0; k < nseg[l]; ++k) {
+        LbOwner& o = own[seg[l][k].j];
+        if (o.n >= 7) { fits = false; break; }
+        o.s[o.n++] = (unsigned char)(2 * l + k);
+      }
+    }
+    if (fits) return true;
+    for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
+    for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
+  }
+  return false;
+}
 static std::mutex g_init_mu;
 
 static int fail(int code, const char* fmt, ...) {
@@ -72,6 +127,18 @@ static int ensure_init(int device) {
   for (int k = 1; k < 256; ++k) inv[k] = 1.0 / (double)k;
   CK(cudaMemcpyToSymbol(c_binom, binom, sizeof(binom)));
   CK(cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)));
+  // La Budde lane schedules for every triangle size (built once, kept for the process lifetime)
+  std::vector<LbLane> lanes((LB_KMAX + 1) * 32);
+  std::vector<LbOwner> own((LB_KMAX + 1) * (LB_KMAX + 1));
+  for (int k = 0; k <= LB_KMAX; ++k)
+    if (!lb_schedule(k, &lanes[k * 32], &own[k * (LB_KMAX + 1)]))
+      return fail(WG_EINVAL, "no La Budde schedule for %d coefficients", k);
+  if (!g_lb_lane) {
+    CK(cudaMalloc(&g_lb_lane, sizeof(LbLane) * lanes.size()));
+    CK(cudaMalloc(&g_lb_own, sizeof(LbOwner) * own.size()));
+  }
+  CK(cudaMemcpy(g_lb_lane, lanes.data(), sizeof(LbLane) * lanes.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g_lb_own, own.data(), sizeof(LbOwner) * own.size(), cudaMemcpyHostToDevice));
   g_device = dev;
   return WG_OK;
 }
@@ -104,6 +171,7 @@ struct wg_plan {
   std::vector<wg::Group> groups;
   int total_out = 0;
   int nparts = 0;
+  long long h2d_bytes = 0;
   int precision = 0;
   void* dmem = nullptr;
   wg::InstDev* d_inst = nullptr;
@@ -390,6 +458,10 @@ static WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int
   off += al(L.ldw * sb);
   L.off_win = off;
   off += al(L.kw * L.kw * sb);
+  L.off_tb = off;
+  off += al(L.kw * sb);
+  L.off_part = off;
+  off += al(64 * sb);
   L.off_ser = off;
   off += al(narr * L.nser * sb);
   L.off_int = off;
@@ -531,6 +603,7 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
     memcpy(host.data() + b_inst + b_chunks + P[i].d.a_off, P[i].ext.data(), P[i].ext.size());
   if (!scales.empty()) memcpy(host.data() + b_inst + b_chunks + b_pool + b_parts, scales.data(), sizeof(double) * scales.size());
   CK(cudaMemcpy(pl->dmem, host.data(), host.size(), cudaMemcpyHostToDevice));
+  pl->h2d_bytes = (long long)host.size();
   CK(cudaMemset(pl->d_counters, 0, b_cnt + b_err));
   return WG_OK;
 }
@@ -539,6 +612,8 @@ static int execute_plan(wg_plan* pl, cudaStream_t st) {
   for (size_t g = 0; g < pl->groups.size(); ++g) {
     const Group& G = pl->groups[g];
     SieveParams p;
+    p.lb_lane = g_lb_lane;
+    p.lb_own = g_lb_own;
     p.inst = pl->d_inst;
     p.chunks = pl->d_chunks + G.chunk_begin;
     p.nchunks = G.chunk_count;
@@ -556,7 +631,7 @@ static int execute_plan(wg_plan* pl, cudaStream_t st) {
   const int ninst = (int)pl->inst.size();
   if (ninst > 0) {
     const int threads = 128;
-    const int blocks = (pl->total_out + threads - 1) / threads;
+    const int blocks = (pl->total_out * 32 + threads - 1) / threads;  // one warp per output
     reduce_kernel<<<std::max(blocks, 1), threads, 0, st>>>(pl->d_inst, ninst, pl->d_partials, pl->d_scales, pl->d_out,
                                                            pl->d_counters, (int)pl->groups.size(), pl->total_out);
     CK(cudaGetLastError());
@@ -659,6 +734,33 @@ int wg_plan_outputs(const wg_plan* plan) { return plan ? plan->total_out : fail(
 
 int wg_plan_kernel_launches(const wg_plan* plan) {
   return plan ? (int)plan->groups.size() + (plan->inst.empty() ? 0 : 1) : fail(WG_EINVAL, "plan is NULL");
+}
+
+int wg_plan_partials(wg_plan* plan, double* out, int capacity, void* stream) {
+  if (!plan) return fail(WG_EINVAL, "plan is NULL");
+  if (!out || capacity < plan->nparts) return plan->nparts;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (plan->nparts > 0)
+    CK(cudaMemcpyAsync(out, plan->d_partials, sizeof(double2) * plan->nparts, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return plan->nparts;
+}
+
+int wg_plan_chunk(const wg_plan* plan, int chunk, int* inst, int* part, long long* t0, long long* t1) {
+  if (!plan || chunk < 0 || chunk >= (int)plan->chunks.size()) return fail(WG_EINVAL, "bad chunk index");
+  const ChunkDev& c = plan->chunks[chunk];
+  if (inst) *inst = c.inst;
+  if (part) *part = c.part;
+  if (t0) *t0 = c.t0;
+  if (t1) *t1 = c.t1;
+  return (int)plan->chunks.size();
+}
+
+int wg_plan_transfer_bytes(const wg_plan* plan, long long* h2d, long long* d2h) {
+  if (!plan) return fail(WG_EINVAL, "plan is NULL");
+  if (h2d) *h2d = plan->h2d_bytes;
+  if (d2h) *d2h = (long long)sizeof(double2) * plan->total_out;
+  return WG_OK;
 }
 
 int wg_plan_destroy(wg_plan* plan) {

@@ -66,11 +66,26 @@ struct WarpLayout {
   int rows;      // tile rows allocated
   int kw;        // La Budde window size (rows and columns)
   int nser;      // series capacity (entries per array)
-  int off_x, off_win, off_ser, off_int;
+  int off_x, off_win, off_tb, off_part, off_ser, off_int;
   int bytes;     // per warp
 };
 
+// La Budde lane schedule for one triangle size Ki (rows with Ki = min(i, Kc) coefficients):
+// the r-sums of coefficients j = 2..Ki are cut into pieces, at most two pieces per lane, so that
+// every lane does about Ki(Ki-1)/64 multiply-adds; piece a is (ja, r = rloa .. rloa+lena-1),
+// piece b likewise.  A lane's partials go to slots 2*lane and 2*lane+1.
+struct LbLane {
+  signed char ja, rloa, lena, jb, rlob, lenb, pad0, pad1;
+};
+// the slots holding the pieces of coefficient j, summed by j's owner lane in this order
+struct LbOwner {
+  unsigned char n, s[7];
+};
+constexpr int LB_KMAX = 64;
+
 struct SieveParams {
+  const LbLane* lb_lane;    // [(LB_KMAX+1) * 32]
+  const LbOwner* lb_own;    // [(LB_KMAX+1) * (LB_KMAX+1)]
   const InstDev* inst;
   const ChunkDev* chunks;
   int nchunks;
@@ -108,6 +123,18 @@ __device__ __forceinline__ S warp_sum(S v) {
   return v;
 }
 
+__device__ __forceinline__ double shfl_up_c(double v, int off) { return __shfl_up_sync(0xffffffffu, v, off); }
+__device__ __forceinline__ dfr shfl_up_c(dfr v, int off) {
+  return {__shfl_up_sync(0xffffffffu, v.hi, off), __shfl_up_sync(0xffffffffu, v.lo, off)};
+}
+template <class S>
+__device__ __forceinline__ S shfl_up_s(S v, int off) {
+  using A = Ar<S>;
+#pragma unroll
+  for (int c = 0; c < A::NC; ++c) A::set_comp(v, c, shfl_up_c(A::comp(v, c), off));
+  return v;
+}
+
 __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
   double t = s + x;
   if (fabs(s) >= fabs(x))
@@ -120,8 +147,15 @@ __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
 // ------------------------------------------------------------------------------------------
 // Hessenberg reduction of the warp's tile by Gaussian elimination with partial pivoting.
 // W is rows x ldw (row-major); the square part is mb x mb; rows mb..rows-1 are extra row
-// vectors that receive the column operations only.  After the call W[j+1][j] is exactly 1
-// (or 0 when the column below the diagonal was zero) for j = 0..mb-2.
+// vectors that receive the column operations only.
+//
+// FP64 scalars (normalised form): each step is the similarity X^-1 W X with X = I + (x - e)e^T,
+// x = (0..0, piv, W[j+2][j], ..)^T, e = e_{j+1}: row j+1 is divided by the pivot and column
+// j+1 becomes W x, so W[j+1][j] ends exactly 1 (or 0 when the column below the diagonal was
+// zero) and La Budde needs no subdiagonal products.  The pivots compound geometrically under
+// this scaling, which FP64's exponent range absorbs but FP32's does not, so
+// double-float scalars use the classic form: multipliers l = W[a][j]/piv (|l| <= 1),
+// W[j+1][j] keeps the pivot and column j+1 += sum_b W[:,b] l_b.
 template <class S, int NS>
 __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, int rows, int ldw) {
   using A = Ar<S>;
@@ -167,11 +201,15 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
     }
     const S piv = W[(j + 1) * ldw + j];
     const S rp = A::recip(piv);
-    for (int b = j + 1 + lane; b < mb; b += 32) xv[b] = (b == j + 1) ? piv : W[b * ldw + j];
-    __syncwarp();
-    // row j+1 /= piv  (the pivot itself becomes 1)
-    for (int c = j + 1 + lane; c < mb; c += 32) W[(j + 1) * ldw + c] = A::mul(W[(j + 1) * ldw + c], rp);
-    if (lane == 0) W[(j + 1) * ldw + j] = A::one();
+    if constexpr (A::fp64) {
+      for (int b = j + 1 + lane; b < mb; b += 32) xv[b] = (b == j + 1) ? piv : W[b * ldw + j];
+      __syncwarp();
+      // row j+1 /= piv  (the pivot itself becomes 1)
+      for (int c = j + 1 + lane; c < mb; c += 32) W[(j + 1) * ldw + c] = A::mul(W[(j + 1) * ldw + c], rp);
+      if (lane == 0) W[(j + 1) * ldw + j] = A::one();
+    } else {
+      for (int b = j + 1 + lane; b < mb; b += 32) xv[b] = (b == j + 1) ? A::one() : A::mul(W[b * ldw + j], rp);
+    }
     __syncwarp();
     // --- phase A: rows j+2..mb-1, cols j+1..mb-1: W[a][b] -= x[a] * W[j+1][b]  (flattened)
     const int w = mb - j - 1;
@@ -234,14 +272,16 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
 }
 
 // ------------------------------------------------------------------------------------------
-// La Budde's recurrence on the unit/zero-subdiagonal Hessenberg block H (block index 1..m maps
-// to tile index nb..nb+m-1).  Writes c[0..Kc] of det(I - eta H) = sum_j c_j eta^j to cpoly.
-//   c[i][j] = c[i-1][j] - H(i,i) c[i-1][j-1] - sum_{r=1}^{j-1} H(i-r,i) c[i-r-1][j-r-1]
-// where the r-sum stops at the last zero subdiagonal entry (charpoly.py:195-282 with all
-// subdiagonal products equal to 1).
+// La Budde's recurrence on the Hessenberg block H (block index 1..m maps to tile index
+// nb..nb+m-1).  Writes c[0..Kc] of det(I - eta H) = sum_j c_j eta^j to cpoly.
+//   c[i][j] = c[i-1][j] - H(i,i) c[i-1][j-1] - sum_{r=1}^{j-1} T_r c[i-r-1][j-r-1],
+//   T_r = H(i-r,i) beta_i beta_{i-1} ... beta_{i-r+1},  beta_k = H(k,k-1)
+// (charpoly.py:195-282).  In the normalised FP64 form every beta is 1 or 0, so T_r is H(i-r,i)
+// up to the last zero beta; otherwise the beta products come from a lane prefix-product scan.
 template <class S>
 __device__ void labudde(const S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __restrict__ win, int kw,
-                        S* __restrict__ cpoly) {
+                        S* __restrict__ tb, S* __restrict__ part, S* __restrict__ cpoly,
+                        const LbLane* __restrict__ lbl, const LbOwner* __restrict__ lbo) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
   for (int jj = lane; jj <= Kc; jj += 32) win[jj] = (jj == 0) ? A::one() : A::zero();
@@ -250,20 +290,60 @@ __device__ void labudde(const S* __restrict__ W, int ldw, int nb, int m, int Kc,
   int prow = 0;  // window slot of row i-1
   for (int i = 1; i <= m; ++i) {
     const int wi = nb + i - 1;
-    if (i >= 2 && A::is_zero(W[wi * ldw + wi - 1])) zlast = i;
-    const int rmax = i - zlast;
+    const int R = (i - 1) < (Kc - 1) ? (i - 1) : (Kc - 1);  // T_r needed for r = 1..R
+    int rcap = R;
+    if constexpr (A::fp64) {
+      if (i >= 2 && A::is_zero(W[wi * ldw + wi - 1])) zlast = i;
+      rcap = (i - zlast) < R ? (i - zlast) : R;
+      for (int r = lane + 1; r <= rcap; r += 32) tb[r] = W[(wi - r) * ldw + wi];
+    } else {
+      S carry = A::one();
+      for (int base = 0; base < R; base += 32) {
+        const int r = base + lane + 1;
+        S b = (r <= R) ? W[(wi - r + 1) * ldw + (wi - r)] : A::one();
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const S y = shfl_up_s(b, off);
+          if (lane >= off) b = A::mul(y, b);
+        }
+        b = A::mul(carry, b);
+        if (r <= R) tb[r] = A::mul(W[(wi - r) * ldw + wi], b);
+        carry = A::shfl(b, 31);
+      }
+    }
+    __syncwarp();
     const S alpha = W[wi * ldw + wi];
     const int Ki = i < Kc ? i : Kc;
     const int crow = prow + 1 == kw ? 0 : prow + 1;
+    // pieces of sum_r T_r c[i-r-1][j-r-1], balanced over the lanes
+    {
+      const LbLane sc = lbl[Ki * 32 + lane];
+      const int lena = sc.lena, tot = sc.lena + sc.lenb;
+      S acc = A::zero(), pa = A::zero();
+      for (int it = 0; it < tot; ++it) {
+        const bool sec = it >= lena;
+        if (it == lena) { pa = acc; acc = A::zero(); }
+        const int j = sec ? sc.jb : sc.ja;
+        const int r = sec ? sc.rlob + (it - lena) : sc.rloa + it;
+        if (r <= rcap) {
+          int slot = prow - r;  // window slot of row i-r-1 (row i-1 is in prow)
+          if (slot < 0) slot += kw;
+          acc = A::fma(tb[r], win[slot * kw + (j - r - 1)], acc);
+        }
+      }
+      if (sc.lenb) {
+        part[2 * lane] = pa;
+        part[2 * lane + 1] = acc;
+      } else {
+        part[2 * lane] = acc;
+      }
+    }
+    __syncwarp();
     for (int jj = lane + 1; jj <= Ki; jj += 32) {
       S val = (jj <= i - 1) ? win[prow * kw + jj] : A::zero();
       val = A::fnma(alpha, win[prow * kw + jj - 1], val);
-      const int rlim = (jj - 1) < rmax ? (jj - 1) : rmax;
-      int slot = prow;  // slot of row i-r-1 for r = 1 is prow - 1
-      for (int r = 1; r <= rlim; ++r) {
-        slot = slot == 0 ? kw - 1 : slot - 1;
-        val = A::fnma(W[(wi - r) * ldw + wi], win[slot * kw + (jj - r - 1)], val);
-      }
+      const LbOwner ow = lbo[Ki * (LB_KMAX + 1) + jj];
+      for (int k = 0; k < ow.n; ++k) val = A::sub(val, part[ow.s[k]]);
       win[crow * kw + jj] = val;
     }
     if (lane == 0) win[crow * kw] = A::one();
@@ -373,6 +453,8 @@ __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
   S* W = reinterpret_cast<S*>(ws);
   S* xv = reinterpret_cast<S*>(ws + L.off_x);
   S* win = reinterpret_cast<S*>(ws + L.off_win);
+  S* tb = reinterpret_cast<S*>(ws + L.off_tb);
+  S* lbpart = reinterpret_cast<S*>(ws + L.off_part);
   S* ser = reinterpret_cast<S*>(ws + L.off_ser);
   int* srow = reinterpret_cast<int*>(ws + L.off_int);
   int* scol = srow + L.rows;
@@ -484,7 +566,7 @@ __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
       hessenberg_elim<S, NS>(W, xv, mb, rows, ldw);
       // characteristic polynomial coefficients of the block
       const int Kc = I.K < m ? I.K : m;
-      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, cpoly);
+      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, tb, lbpart, cpoly, P.lb_lane, P.lb_own);
       const int Gdeg = I.K;  // degree of det^(-1/2) needed
       inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
 
@@ -599,32 +681,61 @@ __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
   }
 }
 
-// One thread per output: Neumaier sum of the instance's chunk partials in chunk order, then the
-// final scale (0.5^(N/2-1) etc., and the undoing of any input prescaling).  The last thread
-// re-arms the work counters for the next execution.
+// sum (s1 + c1) + (s2 + c2) keeping the rounding error of the leading add
+__device__ __forceinline__ void two_sum_merge(double& s, double& c, double s2, double c2) {
+  const double t = s + s2;
+  const double bb = t - s;
+  const double e = (s - (t - bb)) + (s2 - bb);
+  s = t;
+  c = c + c2 + e;
+}
+
+// One warp per output: lane l Neumaier-sums the chunk partials l, l+32, ... in order, then the
+// lanes merge in a fixed butterfly (bitwise reproducible), and the final scale (0.5^(N/2-1)
+// etc., and the undoing of any input prescaling) is applied.  Thread 0 re-arms the work
+// counters for the next execution.
 __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst, const double2* __restrict__ partials,
                               const double* __restrict__ scales, double2* __restrict__ out, unsigned int* counters,
                               int ncounters, int total_out) {
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (tid < total_out) {
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (gw < total_out) {
     // locate the instance (outputs are laid out instance by instance)
     int lo = 0, hi = ninst - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (inst[mid].out_base <= tid) lo = mid; else hi = mid - 1;
+      if (inst[mid].out_base <= gw) lo = mid; else hi = mid - 1;
     }
     const InstDev& I = inst[lo];
-    const int o = tid - I.out_base;
+    const int o = gw - I.out_base;
     double sr = 0, si = 0, cr = 0, ci = 0;
-    for (int c = 0; c < I.nchunks; ++c) {
+    for (int c = lane; c < I.nchunks; c += 32) {
       const double2 v = partials[I.part_base + c * I.nout + o];
       neumaier(sr, cr, v.x);
       neumaier(si, ci, v.y);
     }
-    const double sc = scales[I.scale_base + o];
-    out[tid] = make_double2((sr + cr) * sc, (si + ci) * sc);
+#pragma unroll
+    for (int off = 16; off; off >>= 1) {
+      const double osr = __shfl_xor_sync(0xffffffffu, sr, off), ocr = __shfl_xor_sync(0xffffffffu, cr, off);
+      const double osi = __shfl_xor_sync(0xffffffffu, si, off), oci = __shfl_xor_sync(0xffffffffu, ci, off);
+      if (lane & off) {  // the upper lane adds into the lower lane's sum: same order on both sides
+        double a = osr, b = ocr;
+        two_sum_merge(a, b, sr, cr);
+        sr = a; cr = b;
+        a = osi; b = oci;
+        two_sum_merge(a, b, si, ci);
+        si = a; ci = b;
+      } else {
+        two_sum_merge(sr, cr, osr, ocr);
+        two_sum_merge(si, ci, osi, oci);
+      }
+    }
+    if (lane == 0) {
+      const double sc = scales[I.scale_base + o];
+      out[gw] = make_double2((sr + cr) * sc, (si + ci) * sc);
+    }
   }
-  if (tid == 0)
+  if (blockIdx.x == 0 && threadIdx.x == 0)
     for (int i = 0; i < ncounters; ++i) counters[i] = 0u;
 }
 
