@@ -110,6 +110,21 @@ int wg_run(const wg_instance* inst, int count, int precision, double* out, void*
 /* Device-time microbenchmark of the FP64 and FP32 FMA pipes (TFLOP/s, 2 flops per FMA). */
 int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
 
+/* Allocation-free plain hafnian (FP64 terms).  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory while they call us -- code that runs inside its own
+ * memory pool or arena, serving plugins that forbid allocation on the request path, and loops
+ * where cudaMalloc/cudaFree would stall the device.  Same arguments and result as wg_hafnian,
+ * except that A_dev (the prepared n x n matrix, n = 2E <= 64) and out_dev ({re, im}) are DEVICE
+ * pointers on the current device, and the call only enqueues work on `stream` (synchronise
+ * before reading out_dev).  The working memory it needs beyond its inputs and outputs lives in
+ * a static device array of WG_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
+ * until the process exits; sizes beyond what the kernels or that array hold are rejected with
+ * WG_EINVAL.  The first call on a device sets the array up (make it before any stream capture).
+ * All calls share the array: calls that overlap on the GPU race, so serialise them. */
+#define WG_NOALLOC_SCRATCH_BYTES (512 * 1024)
+int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int64_t* edge_reps, int E, int glynn,
+                       double* out_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,8 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwalrus_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["sieve.cu"]
-DEPS = ["sieve.cu", "sieve_kernel.cuh", "arith.cuh"]
+SOURCES = ["sieve.cu", "noalloc.cu"]
+DEPS = ["sieve.cu", "noalloc.cu", "sieve_kernel.cuh", "arith.cuh", "host_common.h"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-shared"]
 
@@ -86,7 +86,7 @@ EXPORTS = [
     "wg_loop_hafnian_batch", "wg_plan_create", "wg_plan_execute", "wg_plan_read", "wg_plan_outputs",
     "wg_plan_kernel_launches", "wg_plan_partials", "wg_plan_chunk", "wg_plan_transfer_bytes",
     "wg_plan_destroy", "wg_run",
-    "wg_measure_fp_peaks",
+    "wg_measure_fp_peaks", "wg_hafnian_noalloc",
 ]
 
 
@@ -121,6 +121,7 @@ def load(build_if_needed=True):
     lib.wg_plan_destroy.argtypes = [vp]
     lib.wg_run.argtypes = [ctypes.POINTER(WgInstance), i32, i32, dp, vp]
     lib.wg_measure_fp_peaks.argtypes = [dp, dp]
+    lib.wg_hafnian_noalloc.argtypes = [vp, i32, i32, ip, i32, i32, vp, vp]
     _lib = lib
     return lib
 

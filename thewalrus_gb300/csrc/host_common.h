@@ -1,0 +1,119 @@
+// Host-side helpers shared by the translation units that launch the sieve kernels:
+// scalar classes, register classes, per-warp shared-memory layout and the La Budde lane
+// schedule.
+#pragma once
+#include <algorithm>
+#include <vector>
+
+#include "sieve_kernel.cuh"
+
+namespace wg {
+
+// scalar classes
+enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3 };
+static size_t stype_bytes(int st) { return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16; }
+
+static const int NS_CPLX[] = {4, 6, 8, 10};
+static const int NS_REAL[] = {4, 8, 12};
+
+static inline int pick_ns(int stype, int rows) {
+  if (stype == ST_CPLX64 || stype == ST_CPLXDF) {
+    for (int ns : NS_CPLX)
+      if (8 * ns >= rows) return ns;
+  } else {
+    for (int ns : NS_REAL)
+      if (8 * ns >= rows) return ns;
+  }
+  return -1;
+}
+
+static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int narr) {
+  WarpLayout L;
+  const int sb = (int)stype_bytes(stype);
+  auto al = [](int x) { return (x + 15) & ~15; };
+  L.ldw = std::max(mb, 1) | 1;
+  L.rows = std::max(rows, 1);
+  L.kw = kc + 1;
+  L.nser = (nser + 1) & ~1;
+  int off = al(L.rows * L.ldw * sb);
+  L.off_x = off;
+  off += al(L.ldw * sb);
+  L.off_win = off;
+  off += al(L.kw * L.kw * sb);
+  L.off_tb = off;
+  off += al(L.kw * sb);
+  L.off_part = off;
+  off += al(64 * sb);
+  L.off_ser = off;
+  off += al(narr * L.nser * sb);
+  L.off_int = off;
+  off += al((L.rows + 2 * L.ldw) * 4);
+  L.bytes = al(off);
+  return L;
+}
+
+// Balanced La Budde schedule for triangle size Ki: coefficient j (2..Ki) needs j-1 products.
+// Find the smallest per-lane load t for which the pieces (each j's products cut into
+// ceil((j-1)/t) near-equal runs) pack into 32 lanes with at most two pieces per lane
+// (largest piece first, onto the least-loaded lane that fits).
+static inline bool lb_schedule(int Ki, LbLane* lanes, LbOwner* own) {
+  for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
+  for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
+  const int W = Ki * (Ki - 1) / 2;
+  if (W == 0) return true;
+  struct Piece { int j, rlo, len; };
+  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
+    // at most 64 pieces fit (two per lane); fixed storage, no heap allocation
+    int npcs = 0;
+    for (int j = 2; j <= Ki; ++j) npcs += (j - 1 + t - 1) / t;
+    if (npcs > 64) continue;
+    Piece pcs[64];
+    npcs = 0;
+    for (int j = 2; j <= Ki; ++j) {
+      const int x = j - 1, p = (x + t - 1) / t;
+      int r = 1;
+      for (int q = 0; q < p; ++q) {
+        const int len = x / p + (q < x % p ? 1 : 0);
+        pcs[npcs++] = {j, r, len};
+        r += len;
+      }
+    }
+    // stable insertion sort, longest piece first
+    for (int a = 1; a < npcs; ++a) {
+      const Piece key = pcs[a];
+      int b = a - 1;
+      while (b >= 0 && pcs[b].len < key.len) { pcs[b + 1] = pcs[b]; --b; }
+      pcs[b + 1] = key;
+    }
+    int load[32] = {0}, nseg[32] = {0};
+    Piece seg[32][2];
+    bool ok = true;
+    for (int q = 0; q < npcs; ++q) {
+      const Piece& pc = pcs[q];
+      int best = -1;
+      for (int l = 0; l < 32; ++l)
+        if (nseg[l] < 2 && load[l] + pc.len <= t && (best < 0 || load[l] < load[best])) best = l;
+      if (best < 0) { ok = false; break; }
+      seg[best][nseg[best]++] = pc;
+      load[best] += pc.len;
+    }
+    if (!ok) continue;
+    bool fits = true;
+    for (int l = 0; l < 32 && fits; ++l) {
+      LbLane& L = lanes[l];
+      if (nseg[l] > 0) { L.ja = (signed char)seg[l][0].j; L.rloa = (signed char)seg[l][0].rlo; L.lena = (signed char)seg[l][0].len; }
+      if (nseg[l] > 1) { L.jb = (signed char)seg[l][1].j; L.rlob = (signed char)seg[l][1].rlo; L.lenb = (signed char)seg[l][1].len; }
+      for (int k = 0; k < nseg[l]; ++k) {
+        LbOwner& o = own[seg[l][k].j];
+        if (o.n >= 7) { fits = false; break; }
+        o.s[o.n++] = (unsigned char)(2 * l + k);
+      }
+    }
+    if (fits) return true;
+    for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
+    for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
+  }
+  return false;
+}
+
+}  // namespace wg

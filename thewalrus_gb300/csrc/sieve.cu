@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/walrus_gb300.h"
+#include "host_common.h"
 #include "sieve_kernel.cuh"
 
 namespace wg {
@@ -29,59 +30,10 @@ static int g_num_sms = 0;
 static LbLane* g_lb_lane = nullptr;
 static LbOwner* g_lb_own = nullptr;
 
-// Balanced La Budde schedule for triangle size Ki: coefficient j (2..Ki) needs j-1 products.
-// Find the smallest per-lane load t for which the pieces (each j's products cut into
-// ceil((j-1)/t) near-equal runs) pack into 32 lanes with at most two pieces per lane
-// (largest piece first, onto the least-loaded lane that fits).
-static bool lb_schedule(int Ki, LbLane* lanes, LbOwner* own) {
-  for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
-  for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
-  const int W = Ki * (Ki - 1) / 2;
-  if (W == 0) return true;
-  struct Piece { int j, rlo, len; };
-  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
-    std::vector<Piece> pcs;
-    for (int j = 2; j <= Ki; ++j) {
-      const int x = j - 1, p = (x + t - 1) / t;
-      int r = 1;
-      for (int q = 0; q < p; ++q) {
-        const int len = x / p + (q < x % p ? 1 : 0);
-        pcs.push_back({j, r, len});
-        r += len;
-      }
-    }
-    if ((int)pcs.size() > 64) continue;
-    std::stable_sort(pcs.begin(), pcs.end(), [](const Piece& a, const Piece& b) { return a.len > b.len; });
-    int load[32] = {0}, nseg[32] = {0};
-    Piece seg[32][2];
-    bool ok = true;
-    for (const Piece& pc : pcs) {
-      int best = -1;
-      for (int l = 0; l < 32; ++l)
-        if (nseg[l] < 2 && load[l] + pc.len <= t && (best < 0 || load[l] < load[best])) best = l;
-      if (best < 0) { ok = false; break; }
-      seg[best][nseg[best]++] = pc;
-      load[best] += pc.len;
-    }
-    if (!ok) continue;
-    bool fits = true;
-    for (int l = 0; l < 32 && fits; ++l) {
-      LbLane& L = lanes[l];
-      if (nseg[l] > 0) { L.ja = (signed char)seg[l][0].j; L.rloa = (signed char)seg[l][0].rlo; L.lena = (signed char)seg[l][0].len; }
-      if (nseg[l] > 1) { L.jb = (signed char)seg[l][1].j; L.rlob = (signed char)seg[l][1].rlo; L.lenb = (signed char)seg[l][1].len; }
-      for (int k = 0; k < nseg[l]; ++k) {
-        LbOwner& o = own[seg[l][k].j];
-        if (o.n >= 7) { fits = false; break; }
-        o.s[o.n++] = (unsigned char)(2 * l + k);
-      }
-    }
-    if (fits) return true;
-    for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
-    for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
-  }
-  return false;
-}
 static std::mutex g_init_mu;
+
+// lets other translation units of the library report through wg_last_error()
+void set_last_error(const char* msg) { g_err = msg; }
 
 static int fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -143,9 +95,6 @@ static int ensure_init(int device) {
   return WG_OK;
 }
 
-// scalar classes
-enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3 };
-static size_t stype_bytes(int st) { return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16; }
 
 struct Prepared {
   InstDev d;
@@ -186,8 +135,6 @@ struct wg_plan {
 
 namespace wg {
 
-static const int NS_CPLX[] = {4, 6, 8, 10};
-static const int NS_REAL[] = {4, 8, 12};
 
 template <class S, int NS>
 static cudaError_t launch_one(const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
@@ -242,16 +189,6 @@ static int occupancy_one(int wpc, int smem) {
       break;                                                   \
   }
 
-static int pick_ns(int stype, int rows) {
-  if (stype == ST_CPLX64 || stype == ST_CPLXDF) {
-    for (int ns : NS_CPLX)
-      if (8 * ns >= rows) return ns;
-  } else {
-    for (int ns : NS_REAL)
-      if (8 * ns >= rows) return ns;
-  }
-  return -1;
-}
 
 static inline void put_scalar(unsigned char* dst, int st, double re, double im) {
   switch (st) {
@@ -445,30 +382,6 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
   return WG_OK;
 }
 
-static WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int narr) {
-  WarpLayout L;
-  const int sb = (int)stype_bytes(stype);
-  auto al = [](int x) { return (x + 15) & ~15; };
-  L.ldw = std::max(mb, 1) | 1;
-  L.rows = std::max(rows, 1);
-  L.kw = kc + 1;
-  L.nser = (nser + 1) & ~1;
-  int off = al(L.rows * L.ldw * sb);
-  L.off_x = off;
-  off += al(L.ldw * sb);
-  L.off_win = off;
-  off += al(L.kw * L.kw * sb);
-  L.off_tb = off;
-  off += al(L.kw * sb);
-  L.off_part = off;
-  off += al(64 * sb);
-  L.off_ser = off;
-  off += al(narr * L.nser * sb);
-  L.off_int = off;
-  off += al((L.rows + 2 * L.ldw) * 4);
-  L.bytes = al(off);
-  return L;
-}
 
 static int build_plan(const wg_instance* v, int count, int precision, double chunk_scale, wg_plan* pl) {
   if (count < 0 || (count > 0 && !v)) return fail(WG_EINVAL, "bad instance list");

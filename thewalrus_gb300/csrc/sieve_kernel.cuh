@@ -96,8 +96,9 @@ struct SieveParams {
   WarpLayout L;
 };
 
-__constant__ double c_binom[BINOM_N][BINOM_N];
-__constant__ double c_inv[256];  // c_inv[k] = 1/k (k >= 1)
+// internal linkage: every translation unit that launches the kernels owns its tables
+static __constant__ double c_binom[BINOM_N][BINOM_N];
+static __constant__ double c_inv[256];  // c_inv[k] = 1/k (k >= 1)
 
 __device__ __forceinline__ double inv_int(int k) { return k < 256 ? c_inv[k] : 1.0 / (double)k; }
 
@@ -443,7 +444,7 @@ __device__ void loop_krylov(const S* __restrict__ W, int ldw, int m, int mb, int
 
 // ------------------------------------------------------------------------------------------
 template <class S, int NS>
-__global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
+static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
   using A = Ar<S>;
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
@@ -694,7 +695,7 @@ __device__ __forceinline__ void two_sum_merge(double& s, double& c, double s2, d
 // lanes merge in a fixed butterfly (bitwise reproducible), and the final scale (0.5^(N/2-1)
 // etc., and the undoing of any input prescaling) is applied.  Thread 0 re-arms the work
 // counters for the next execution.
-__global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst, const double2* __restrict__ partials,
+static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst, const double2* __restrict__ partials,
                               const double* __restrict__ scales, double2* __restrict__ out, unsigned int* counters,
                               int ncounters, int total_out) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
