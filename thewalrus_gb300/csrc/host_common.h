@@ -27,7 +27,8 @@ static inline int pick_ns(int stype, int rows) {
   return -1;
 }
 
-static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int narr) {
+// tilewin: La Budde's coefficient rows live in dead tile columns (only rows 0..2 need `win`)
+static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int narr, bool tilewin) {
   WarpLayout L;
   const int sb = (int)stype_bytes(stype);
   auto al = [](int x) { return (x + 15) & ~15; };
@@ -39,7 +40,8 @@ static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int ns
   L.off_x = off;
   off += al(L.ldw * sb);
   L.off_win = off;
-  off += al(L.kw * L.kw * sb);
+  L.tilewin = tilewin ? 1 : 0;
+  off += al((tilewin ? 3 : L.kw) * L.kw * sb);
   L.off_tb = off;
   off += al(L.kw * sb);
   L.off_part = off;

@@ -100,6 +100,7 @@ struct Prepared {
   InstDev d;
   int stype;
   int rows_max, mb_max, m_max, kc_max, nser_need, narr;
+  bool tile_ok;  // every term can keep its La Budde rows in dead tile columns
   double term_cost;
   std::vector<double> scales;
   std::vector<unsigned char> ext;  // extended matrix in the kernel's scalar type
@@ -338,6 +339,13 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
   P.kc_max = std::min(d.K, m_max);
   P.nser_need = std::max(std::max(d.K, d.Nodd), std::max(Nf, m_max)) + 2;
   P.narr = (kind == KIND_PLAIN) ? 2 : 8;
+  {
+    // a term with m < K+1 and no border/extra rows has columns shorter than Kc+1: only when
+    // some delta can vanish (an even repetition, or inclusion/exclusion)
+    bool all_odd = d.glynn != 0;
+    for (int r : reps) all_odd = all_odd && (r % 2 == 1);
+    P.tile_ok = (nb + ne >= 1) || (all_odd && d.K < m_max);
+  }
   P.term_cost = (double)P.mb_max * P.mb_max * P.mb_max + 64.0;
   if (P.rows_max > 80) return fail(WG_EINVAL, "term matrix of %d rows above the supported 80", P.rows_max);
   if (P.kc_max > 64) return fail(WG_EINVAL, "more than 64 characteristic coefficients");
@@ -428,6 +436,7 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
     G.stype = keys[g].st;
     G.ns = keys[g].ns;
     int rows = 1, mb = 1, kc = 0, nser = 2, narr = 2;
+    bool tile = true;
     double total_cost = 0;
     std::vector<int> members;
     for (int i = 0; i < count; ++i)
@@ -438,9 +447,10 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
         kc = std::max(kc, P[i].kc_max);
         nser = std::max(nser, P[i].nser_need);
         narr = std::max(narr, P[i].narr);
+        tile = tile && P[i].tile_ok;
         total_cost += P[i].term_cost * (double)P[i].d.steps;
       }
-    G.L = make_layout(G.stype, rows, mb, kc, nser, narr);
+    G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
     const int max_smem = 227 * 1024;
     int wpc = std::min(8, max_smem / G.L.bytes);
     if (wpc < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);

@@ -67,6 +67,7 @@ struct WarpLayout {
   int kw;        // La Budde window size (rows and columns)
   int nser;      // series capacity (entries per array)
   int off_x, off_win, off_tb, off_part, off_ser, off_int;
+  int tilewin;   // La Budde rows kept in dead tile columns (win then holds rows 0..2 only)
   int bytes;     // per warp
 };
 
@@ -218,11 +219,23 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
       const int dr = 32 / w, dc = 32 % w;
       int a = j + 2 + lane / w, b = j + 1 + lane % w;
       const S* prow = W + (j + 1) * ldw;
-      while (a < mb) {
-        W[a * ldw + b] = A::fnma(xv[a], prow[b], W[a * ldw + b]);
-        b += dc;
-        a += dr;
-        if (b >= mb) { b -= w; a += 1; }
+      while (a < mb) {  // four independent elements per pass: loads issued before the stores
+        int aa[4], bb[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          aa[u] = a;
+          bb[u] = b;
+          b += dc;
+          a += dr;
+          if (b >= mb) { b -= w; a += 1; }
+        }
+        S vv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (aa[u] < mb) vv[u] = A::fnma(xv[aa[u]], prow[bb[u]], W[aa[u] * ldw + bb[u]]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (aa[u] < mb) W[aa[u] * ldw + bb[u]] = vv[u];
       }
     }
     __syncwarp();
@@ -273,6 +286,16 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
 }
 
 // ------------------------------------------------------------------------------------------
+// Storage of La Budde's coefficient rows c[i'][0..Kc].  Tile mode: rows 0..2 live in `win`
+// (3 x kw) and row i' >= 3 down block column i'-2 of the tile, which is dead by then (column c
+// is last read at step c+1, the subdiagonal entries being cached); otherwise a circular window of
+// kw rows (slot = i' mod kw) when the tile cannot hold Kc+1 entries per column.
+template <class S>
+__device__ __forceinline__ S& cw_at(S* W, int ldw, int nb, S* win, int kw, bool tile, int ip, int slot, int u) {
+  if (tile) return ip >= 3 ? W[u * ldw + nb + ip - 3] : win[ip * kw + u];
+  return win[slot * kw + u];
+}
+
 // La Budde's recurrence on the Hessenberg block H (block index 1..m maps to tile index
 // nb..nb+m-1).  Writes c[0..Kc] of det(I - eta H) = sum_j c_j eta^j to cpoly.
 //   c[i][j] = c[i-1][j] - H(i,i) c[i-1][j-1] - sum_{r=1}^{j-1} T_r c[i-r-1][j-r-1],
@@ -280,58 +303,62 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
 // (charpoly.py:195-282).  In the normalised FP64 form every beta is 1 or 0, so T_r is H(i-r,i)
 // up to the last zero beta; otherwise the beta products come from a lane prefix-product scan.
 template <class S>
-__device__ void labudde(const S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __restrict__ win, int kw,
-                        S* __restrict__ tb, S* __restrict__ part, S* __restrict__ cpoly,
+__device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __restrict__ win, int kw, bool tile,
+                        S* __restrict__ bet, S* __restrict__ tb, S* __restrict__ part, S* __restrict__ cpoly,
                         const LbLane* __restrict__ lbl, const LbOwner* __restrict__ lbo) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
-  for (int jj = lane; jj <= Kc; jj += 32) win[jj] = (jj == 0) ? A::one() : A::zero();
+  for (int k = lane + 2; k <= m; k += 32) bet[k] = W[(nb + k - 1) * ldw + nb + k - 2];
+  for (int jj = lane; jj <= Kc; jj += 32) cw_at(W, ldw, nb, win, kw, tile, 0, 0, jj) = (jj == 0) ? A::one() : A::zero();
   __syncwarp();
   int zlast = 1;
-  int prow = 0;  // window slot of row i-1
+  int prow = 0;  // circular-window slot of row i-1
+  // subdiagonal products P(i, r) = beta_i ... beta_{i-r+1} for r = lane+1 and lane+33, kept in
+  // registers across rows: P(i, r) = beta_i * P(i-1, r-1), P(i, 1) = beta_i
+  S pr0 = A::zero(), pr1 = A::zero();
   for (int i = 1; i <= m; ++i) {
     const int wi = nb + i - 1;
     const int R = (i - 1) < (Kc - 1) ? (i - 1) : (Kc - 1);  // T_r needed for r = 1..R
     int rcap = R;
     if constexpr (A::fp64) {
-      if (i >= 2 && A::is_zero(W[wi * ldw + wi - 1])) zlast = i;
+      if (i >= 2 && A::is_zero(bet[i])) zlast = i;
       rcap = (i - zlast) < R ? (i - zlast) : R;
       for (int r = lane + 1; r <= rcap; r += 32) tb[r] = W[(wi - r) * ldw + wi];
     } else {
-      S carry = A::one();
-      for (int base = 0; base < R; base += 32) {
-        const int r = base + lane + 1;
-        S b = (r <= R) ? W[(wi - r + 1) * ldw + (wi - r)] : A::one();
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-          const S y = shfl_up_s(b, off);
-          if (lane >= off) b = A::mul(y, b);
-        }
-        b = A::mul(carry, b);
-        if (r <= R) tb[r] = A::mul(W[(wi - r) * ldw + wi], b);
-        carry = A::shfl(b, 31);
-      }
+      const S bi = i >= 2 ? bet[i] : A::zero();
+      const S up0 = shfl_up_s(pr0, 1);  // P(i-1, r-1) for r = lane+1
+      const S up1 = shfl_up_s(pr1, 1);
+      const S last0 = A::shfl(pr0, 31);  // P(i-1, 32) feeds r = 33
+      const S prev0 = lane == 0 ? A::one() : up0;
+      const S prev1 = lane == 0 ? last0 : up1;
+      pr0 = A::mul(bi, prev0);
+      pr1 = A::mul(bi, prev1);
+      if (lane + 1 <= R) tb[lane + 1] = A::mul(W[(wi - lane - 1) * ldw + wi], pr0);
+      if (lane + 33 <= R) tb[lane + 33] = A::mul(W[(wi - lane - 33) * ldw + wi], pr1);
     }
     __syncwarp();
     const S alpha = W[wi * ldw + wi];
     const int Ki = i < Kc ? i : Kc;
     const int crow = prow + 1 == kw ? 0 : prow + 1;
-    // pieces of sum_r T_r c[i-r-1][j-r-1], balanced over the lanes
+    // pieces of sum_r T_r c[i-r-1][j-r-1], balanced over the lanes (two accumulators for ILP)
     {
       const LbLane sc = lbl[Ki * 32 + lane];
       const int lena = sc.lena, tot = sc.lena + sc.lenb;
-      S acc = A::zero(), pa = A::zero();
+      S acc0 = A::zero(), acc1 = A::zero(), pa = A::zero();
       for (int it = 0; it < tot; ++it) {
         const bool sec = it >= lena;
-        if (it == lena) { pa = acc; acc = A::zero(); }
+        if (it == lena) { pa = A::add(acc0, acc1); acc0 = A::zero(); acc1 = A::zero(); }
         const int j = sec ? sc.jb : sc.ja;
         const int r = sec ? sc.rlob + (it - lena) : sc.rloa + it;
         if (r <= rcap) {
-          int slot = prow - r;  // window slot of row i-r-1 (row i-1 is in prow)
+          int slot = prow - r;  // circular slot of row i-r-1 (row i-1 is in prow)
           if (slot < 0) slot += kw;
-          acc = A::fma(tb[r], win[slot * kw + (j - r - 1)], acc);
+          const S cv = cw_at(W, ldw, nb, win, kw, tile, i - r - 1, slot, j - r - 1);
+          if (it & 1) acc1 = A::fma(tb[r], cv, acc1);
+          else acc0 = A::fma(tb[r], cv, acc0);
         }
       }
+      const S acc = A::add(acc0, acc1);
       if (sc.lenb) {
         part[2 * lane] = pa;
         part[2 * lane + 1] = acc;
@@ -341,17 +368,17 @@ __device__ void labudde(const S* __restrict__ W, int ldw, int nb, int m, int Kc,
     }
     __syncwarp();
     for (int jj = lane + 1; jj <= Ki; jj += 32) {
-      S val = (jj <= i - 1) ? win[prow * kw + jj] : A::zero();
-      val = A::fnma(alpha, win[prow * kw + jj - 1], val);
+      S val = (jj <= i - 1) ? cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj) : A::zero();
+      val = A::fnma(alpha, cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj - 1), val);
       const LbOwner ow = lbo[Ki * (LB_KMAX + 1) + jj];
       for (int k = 0; k < ow.n; ++k) val = A::sub(val, part[ow.s[k]]);
-      win[crow * kw + jj] = val;
+      cw_at(W, ldw, nb, win, kw, tile, i, crow, jj) = val;
     }
-    if (lane == 0) win[crow * kw] = A::one();
+    if (lane == 0) cw_at(W, ldw, nb, win, kw, tile, i, crow, 0) = A::one();
     prow = crow;
     __syncwarp();
   }
-  for (int jj = lane; jj <= Kc; jj += 32) cpoly[jj] = win[prow * kw + jj];
+  for (int jj = lane; jj <= Kc; jj += 32) cpoly[jj] = cw_at(W, ldw, nb, win, kw, tile, m, prow, jj);
   __syncwarp();
 }
 
@@ -565,9 +592,11 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       }
       __syncwarp();
       hessenberg_elim<S, NS>(W, xv, mb, rows, ldw);
-      // characteristic polynomial coefficients of the block
+      // loop variants: Krylov data of the border first (La Budde then reuses the tile)
+      if (kind != KIND_PLAIN) loop_krylov<S>(W, ldw, m, mb, ne, I.K, xv, eser, lam, mu, mu0);
+      // characteristic polynomial coefficients of the block (xv caches the subdiagonal)
       const int Kc = I.K < m ? I.K : m;
-      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, tb, lbpart, cpoly, P.lb_lane, P.lb_own);
+      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, L.tilewin != 0, xv, tb, lbpart, cpoly, P.lb_lane, P.lb_own);
       const int Gdeg = I.K;  // degree of det^(-1/2) needed
       inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
 
@@ -581,7 +610,6 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
         }
       } else {
         const int T = I.K;
-        loop_krylov<S>(W, ldw, m, mb, ne, T, xv, eser, lam, mu, mu0);  // xv is free after the reduction
         // even series: q_l = lam_l / 2, e = exp(q), f_even[h] = sum_t g_t e_{h-t}
         if (kind == KIND_LOOP || kind == KIND_BATCH_EVEN || kind == KIND_BATCH_ODD) {
           for (int l = lane; l <= T; l += 32) qv[l] = l ? A::scale(lam[l], 0.5) : A::zero();
