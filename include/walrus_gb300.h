@@ -91,6 +91,28 @@ int wg_loop_hafnian_batch(const void* A, const void* D, int n, int dtype, const 
  *   wg_plan_read   : copy all outputs (instance order, complex interleaved) to the host
  * chunk_scale (>0) multiplies the default chunks-per-warp target (1.0 = default). */
 int wg_plan_create(const wg_instance* inst, int count, int precision, double chunk_scale, wg_plan** plan);
+
+/* Tuning knobs of a plan (zero-initialised fields take the defaults):
+ *   chunk_scale       chunks per resident warp relative to the default 4 (term-chunk size)
+ *   max_warps_per_cta cap on warps per CTA (default: as many as shared memory allows, <= 8)
+ *   merge_classes     1: one persistent launch per scalar type instead of per register class
+ *   use_graph         1: wg_plan_execute captures its launches into a CUDA graph on first use
+ *                        and replays the graph afterwards
+ *   stream            non-NULL: the plan's memory comes from the stream-ordered allocator and
+ *                     its uploads run on this stream without any device-wide synchronisation
+ *                     (for serving loops that build plans while others execute); the plan must
+ *                     then execute on this stream, and its memory returns to the pool in stream
+ *                     order at destruction */
+typedef struct wg_plan_options {
+  double chunk_scale;
+  int32_t max_warps_per_cta;
+  int32_t merge_classes;
+  int32_t use_graph;
+  int32_t reserved;
+  void* stream;
+} wg_plan_options;
+int wg_plan_create_ex(const wg_instance* inst, int count, int precision, const wg_plan_options* options,
+                      wg_plan** plan);
 int wg_plan_execute(wg_plan* plan, void* stream);
 int wg_plan_read(wg_plan* plan, double* out, void* stream);
 int wg_plan_outputs(const wg_plan* plan);
@@ -106,6 +128,29 @@ int wg_plan_transfer_bytes(const wg_plan* plan, long long* h2d, long long* d2h);
 int wg_plan_destroy(wg_plan* plan);
 /* create + execute + read + destroy */
 int wg_run(const wg_instance* inst, int count, int precision, double* out, void* stream);
+
+/* Serving: a Gaussian state resident on the device and plans whose loop-hafnian matrices are
+ * formed on the device from it.  No single counterpart in the reference: it replaces the host
+ * work of thewalrus/quantum/fock_tensors.py:74-92 (reduction of B and gamma by the photon
+ * pattern) followed by hafnian_repeated / hafnian(loop=True).
+ *   wg_state_create : upload B (M x M complex128) and gamma (M complex128) once per state
+ *   wg_plan_create_requests : one loop-hafnian instance per request; request r lists its
+ *     pairing (x: 2E mode indices, vertex i paired with i+E, as matched_reps returns them), its
+ *     edge multiplicities and its unpaired mode (-1 if none); a gather kernel writes
+ *     B[x][:, x], gamma[x] and, for an unpaired mode o, B[o, x] and gamma[o] into the pool. */
+typedef struct wg_state wg_state;
+typedef struct wg_request {
+  const int32_t* x;          /* 2E mode indices */
+  const int64_t* edge_reps;  /* E multiplicities */
+  int32_t E;
+  int32_t oddmode;           /* unpaired mode or -1 */
+} wg_request;
+int wg_state_create(const double* B, const double* gamma, int M, wg_state** state);
+int wg_state_destroy(wg_state* state);
+int wg_plan_create_requests(const wg_state* state, const wg_request* req, int count, int precision,
+                            const wg_plan_options* options, wg_plan** plan);
+/* Device bytes a plan holds (for admission control). */
+long long wg_plan_device_bytes(const wg_plan* plan);
 
 /* Device-time microbenchmark of the FP64 and FP32 FMA pipes (TFLOP/s, 2 flops per FMA). */
 int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);

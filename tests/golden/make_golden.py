@@ -26,7 +26,13 @@ from thewalrus_gb300 import workloads as wl  # noqa: E402
 
 
 def import_reference(path):
-    stub = types.ModuleType("numba")
+    def mk(name):
+        m = types.ModuleType(name)
+        m.__path__ = []
+        sys.modules[name] = m
+        return m
+
+    stub = mk("numba")
 
     def jit(*args, **kwargs):
         if args and callable(args[0]) and not kwargs:
@@ -36,7 +42,12 @@ def import_reference(path):
     stub.jit = jit
     stub.njit = jit
     stub.prange = range
-    sys.modules["numba"] = stub
+    # the quantum package imports a numba tuple helper and dask; plain-Python stand-ins suffice
+    mk("numba.cpython")
+    mk("numba.cpython.unsafe")
+    mk("numba.cpython.unsafe.tuple").tuple_setitem = lambda t, i, v: t[:i] + (v,) + t[i + 1:]
+    dask = mk("dask")
+    dask.delayed = lambda f: f
     pkg = types.ModuleType("thewalrus")
     pkg.__path__ = [os.path.join(path, "thewalrus")]
     sys.modules["thewalrus"] = pkg
@@ -44,6 +55,13 @@ def import_reference(path):
     import thewalrus._hafnian as hf
     import thewalrus.loop_hafnian_batch as lb
     import thewalrus.reference as ref
+    import thewalrus._hermite_multidimensional as hm
+
+    for name in ("hafnian", "hafnian_repeated", "reduction"):
+        setattr(pkg, name, getattr(hf, name))
+    for name in dir(hm):
+        if not name.startswith("_"):
+            setattr(pkg, name, getattr(hm, name))
 
     orig = cp.powertrace
 
@@ -150,6 +168,23 @@ def main():
     for m in (2, 5, 9):
         H = rng.normal(size=(m, m)) + 1j * rng.normal(size=(m, m))
         put("charpoly", H=H, out=np.array(cp.charpoly(H.copy())))
+
+    # pure-state Fock amplitudes (thewalrus/quantum/fock_tensors.py:45-98) of a displaced,
+    # squeezed 6-mode state: cov = S S^T with S = interferometer(U) squeezing(r), hbar = 2
+    import thewalrus.symplectic as sy
+    from thewalrus.quantum.fock_tensors import pure_state_amplitude
+
+    M = 6
+    U = wl.haar_unitary(M, np.random.default_rng(41))
+    r = np.random.default_rng(42).uniform(0.3, 0.8, size=M)
+    S = sy.interferometer(U) @ sy.squeezing(r)
+    cov = S @ S.T
+    mu = np.random.default_rng(43).normal(size=2 * M) * 0.4
+    for case in range(10):
+        pat = rng.integers(0, 3, size=M)
+        if pat.sum() < 2:
+            pat[0] += 2
+        put("pure", mu=mu, cov=cov, pattern=pat, out=pure_state_amplitude(mu, cov, list(pat)))
 
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
     print("wrote %d arrays for %s in %.1fs" % (len(out), counts, time.time() - t0))

@@ -1,0 +1,53 @@
+"""GPU tests of the serving subsystem: matrices formed on the device from a resident state,
+continuous batching over streams, each result the same alone and in the mix (FP64, 1e-10)."""
+import numpy as np
+import pytest
+
+import oracle
+from thewalrus_gb300.serving import GaussianState, ProbabilityServer, poisson_requests
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def test_served_amplitudes_match_reference(golden):
+    pytest.importorskip("torch")
+    cases = golden["pure"]
+    st = GaussianState.from_cov(cases[0]["mu"], cases[0]["cov"])
+    srv = ProbabilityServer([st], max_batch=4, streams=2)
+    reqs = [(0.0, 0, np.asarray(c["pattern"])) for c in cases]
+    res = srv.serve(reqs)
+    for c, r in zip(cases, res):
+        ref = complex(c["out"])
+        assert abs(r["amplitude"] - ref) <= RTOL * abs(ref)
+        assert abs(r["probability"] - abs(ref) ** 2) <= 2 * RTOL * abs(ref) ** 2
+
+
+def test_same_alone_and_in_the_mix():
+    pytest.importorskip("torch")
+    states = [GaussianState.synthetic(modes=24, seed=s) for s in range(3)]
+    reqs = poisson_requests(states, rate=2000.0, count=40, photons=(2, 16), seed=7)
+    srv = ProbabilityServer(states, max_batch=8, streams=3)
+    mixed = srv.serve(reqs)
+    assert len({r["batch"] for r in mixed if r["batch"] >= 0}) > 1
+    for j in range(0, len(reqs), 5):
+        alone = srv.serve([(0.0, reqs[j][1], reqs[j][2])])[0]
+        a, b = alone["probability"], mixed[j]["probability"]
+        assert abs(a - b) <= RTOL * abs(a), (j, a, b)
+    # and against the CPU oracle for a few requests
+    for j in (0, 11, 23):
+        _, s, pat = reqs[j]
+        lh = complex(oracle.hafnian_repeated(states[s].B, list(pat), mu=states[s].gamma, loop=True, precision="long"))
+        ref = abs(lh * states[s].norm(pat)) ** 2
+        assert abs(mixed[j]["probability"] - ref) <= RTOL * ref
+
+
+def test_admission_respects_memory_budget():
+    pytest.importorskip("torch")
+    states = [GaussianState.synthetic(modes=16, seed=9)]
+    reqs = poisson_requests(states, rate=1e6, count=12, photons=(6, 10), seed=3)
+    tight = ProbabilityServer.estimate_bytes(10) + 1  # one request per batch fits
+    srv = ProbabilityServer(states, max_batch=64, streams=2, mem_budget=tight)
+    res = srv.serve(reqs)
+    assert len({r["batch"] for r in res}) == len(reqs)

@@ -18,7 +18,7 @@ def header_symbols():
     for f in os.listdir(inc):
         if f.endswith(".h"):
             src = open(os.path.join(inc, f)).read()
-            syms |= set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(wg_\w+)\s*\(", src, re.M))
+            syms |= set(re.findall(r"^\s*(?:const\s+)?(?:\w+[\s*]+)+(wg_\w+)\s*\(", src, re.M))
     return syms
 
 

@@ -50,13 +50,27 @@ def build(force=False, verbose=False):
         if not force and not _stale():
             return LIB
         os.makedirs(BUILD, exist_ok=True)
-        tmp = LIB + ".tmp%d" % os.getpid()
-        cmd = [_nvcc()] + NVCC_FLAGS + ["-o", tmp] + [os.path.join(CSRC, s) for s in SOURCES]
+        tag = "%d" % os.getpid()
+        compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
+        procs, objs = [], []
+        for src in SOURCES:  # translation units compile in parallel, then one link
+            obj = os.path.join(BUILD, src.replace(".cu", ".%s.o" % tag))
+            cmd = [_nvcc()] + compile_flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+            procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+            objs.append(obj)
+        for cmd, p in procs:
+            out, _ = p.communicate()
+            if p.returncode != 0:
+                raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), out.decode()))
+            if verbose and out:
+                print(out.decode())
+        tmp = LIB + ".tmp" + tag
+        cmd = [_nvcc(), "-shared", "-o", tmp] + objs
         res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
         if res.returncode != 0:
-            raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), res.stdout.decode()))
-        if verbose and res.stdout:
-            print(res.stdout.decode())
+            raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), res.stdout.decode()))
+        for obj in objs:
+            os.unlink(obj)
         os.replace(tmp, LIB)
         return LIB
 
@@ -83,11 +97,23 @@ class WgInstance(ctypes.Structure):
 
 EXPORTS = [
     "wg_init", "wg_last_error", "wg_instance_outputs", "wg_hafnian", "wg_loop_hafnian",
-    "wg_loop_hafnian_batch", "wg_plan_create", "wg_plan_execute", "wg_plan_read", "wg_plan_outputs",
+    "wg_loop_hafnian_batch", "wg_plan_create", "wg_plan_create_ex", "wg_plan_execute", "wg_plan_read", "wg_plan_outputs",
     "wg_plan_kernel_launches", "wg_plan_partials", "wg_plan_chunk", "wg_plan_transfer_bytes",
     "wg_plan_destroy", "wg_run",
-    "wg_measure_fp_peaks", "wg_hafnian_noalloc",
+    "wg_measure_fp_peaks", "wg_hafnian_noalloc", "wg_state_create", "wg_state_destroy",
+    "wg_plan_create_requests", "wg_plan_device_bytes",
 ]
+
+
+class WgRequest(ctypes.Structure):
+    """Mirror of ``wg_request``."""
+
+    _fields_ = [
+        ("x", ctypes.c_void_p),
+        ("edge_reps", ctypes.c_void_p),
+        ("E", ctypes.c_int32),
+        ("oddmode", ctypes.c_int32),
+    ]
 
 
 def load(build_if_needed=True):
@@ -110,6 +136,8 @@ def load(build_if_needed=True):
     lib.wg_loop_hafnian_batch.argtypes = [vp, vp, i32, i32, ip, i32, i32, i32, i32, i32, i32, dp, vp]
     lib.wg_plan_create.argtypes = [ctypes.POINTER(WgInstance), i32, i32, ctypes.c_double,
                                    ctypes.POINTER(vp)]
+    lib.wg_plan_create_ex.argtypes = [ctypes.POINTER(WgInstance), i32, i32, ctypes.POINTER(WgPlanOptions),
+                                      ctypes.POINTER(vp)]
     lib.wg_plan_execute.argtypes = [vp, vp]
     lib.wg_plan_read.argtypes = [vp, dp, vp]
     lib.wg_plan_outputs.argtypes = [vp]
@@ -122,6 +150,12 @@ def load(build_if_needed=True):
     lib.wg_run.argtypes = [ctypes.POINTER(WgInstance), i32, i32, dp, vp]
     lib.wg_measure_fp_peaks.argtypes = [dp, dp]
     lib.wg_hafnian_noalloc.argtypes = [vp, i32, i32, ip, i32, i32, vp, vp]
+    lib.wg_state_create.argtypes = [dp, dp, i32, ctypes.POINTER(vp)]
+    lib.wg_state_destroy.argtypes = [vp]
+    lib.wg_plan_create_requests.argtypes = [vp, ctypes.POINTER(WgRequest), i32, i32,
+                                            ctypes.POINTER(WgPlanOptions), ctypes.POINTER(vp)]
+    lib.wg_plan_device_bytes.argtypes = [vp]
+    lib.wg_plan_device_bytes.restype = ctypes.c_longlong
     _lib = lib
     return lib
 
@@ -173,22 +207,71 @@ class Instance:
         return 1
 
 
-class Plan:
-    """Device-resident batch of instances: create once, execute many times, read results."""
+class WgPlanOptions(ctypes.Structure):
+    """Mirror of ``wg_plan_options``."""
 
-    def __init__(self, instances, precision="fp64", chunk_scale=1.0):
+    _fields_ = [
+        ("chunk_scale", ctypes.c_double),
+        ("max_warps_per_cta", ctypes.c_int32),
+        ("merge_classes", ctypes.c_int32),
+        ("use_graph", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("stream", ctypes.c_void_p),
+    ]
+
+
+class Plan:
+    """Device-resident batch of instances: create once, execute many times, read results.
+
+    ``chunk_scale`` (term-chunk size), ``max_warps_per_cta``, ``merge_classes`` (one persistent
+    launch per scalar type) and ``use_graph`` (CUDA-graph replay) map to ``wg_plan_options``.
+    """
+
+    def __init__(self, instances, precision="fp64", chunk_scale=1.0, max_warps_per_cta=0,
+                 merge_classes=False, use_graph=False):
         self.lib = load()
         self.instances = list(instances)
         arr = (WgInstance * max(len(self.instances), 1))()
         for i, inst in enumerate(self.instances):
             arr[i] = inst.struct
         self._arr = arr
+        opt = WgPlanOptions(float(chunk_scale), int(max_warps_per_cta), int(bool(merge_classes)),
+                            int(bool(use_graph)), 0, None)
         h = ctypes.c_void_p()
-        check(self.lib.wg_plan_create(arr, len(self.instances), PRECISIONS[precision],
-                                      float(chunk_scale), ctypes.byref(h)))
+        check(self.lib.wg_plan_create_ex(arr, len(self.instances), PRECISIONS[precision],
+                                         ctypes.byref(opt), ctypes.byref(h)))
         self.handle = h
         self.total_out = self.lib.wg_plan_outputs(h)
         self.kernel_launches = self.lib.wg_plan_kernel_launches(h)
+
+    @classmethod
+    def from_requests(cls, state, requests, precision="fp64", **options):
+        """Plan over serving requests on a resident state; ``requests`` are (x, edge_reps,
+        oddmode) triples as ``matched_reps`` returns them for each photon pattern."""
+        self = cls.__new__(cls)
+        self.lib = load()
+        self.instances = []
+        keep = []
+        arr = (WgRequest * max(len(requests), 1))()
+        for i, (x, reps, odd) in enumerate(requests):
+            xa = np.ascontiguousarray(x, dtype=np.int32)
+            ra = np.ascontiguousarray(reps, dtype=np.int64)
+            keep.append((xa, ra))
+            arr[i] = WgRequest(xa.ctypes.data, ra.ctypes.data, len(ra), -1 if odd is None else int(odd))
+        self._keep, self._arr = keep, arr
+        opt = WgPlanOptions(float(options.get("chunk_scale", 1.0)), int(options.get("max_warps_per_cta", 0)),
+                            int(bool(options.get("merge_classes", False))), int(bool(options.get("use_graph", False))), 0,
+                            options.get("stream"))
+        h = ctypes.c_void_p()
+        check(self.lib.wg_plan_create_requests(state.handle, arr, len(requests), PRECISIONS[precision],
+                                               ctypes.byref(opt), ctypes.byref(h)))
+        self.handle = h
+        self.total_out = self.lib.wg_plan_outputs(h)
+        self.kernel_launches = self.lib.wg_plan_kernel_launches(h)
+        return self
+
+    def device_bytes(self):
+        return int(self.lib.wg_plan_device_bytes(self.handle))
 
     def transfer_bytes(self):
         h, d = ctypes.c_longlong(), ctypes.c_longlong()
@@ -257,3 +340,28 @@ def measure_fp_peaks():
     a, b = ctypes.c_double(), ctypes.c_double()
     check(lib.wg_measure_fp_peaks(ctypes.byref(a), ctypes.byref(b)))
     return a.value, b.value
+
+
+class DeviceState:
+    """A loop-hafnian source matrix B (M x M) and loop weights gamma (M) resident on the GPU."""
+
+    def __init__(self, B, gamma):
+        self.lib = load()
+        B = np.ascontiguousarray(B, dtype=np.complex128)
+        g = np.ascontiguousarray(gamma, dtype=np.complex128)
+        h = ctypes.c_void_p()
+        dp = ctypes.POINTER(ctypes.c_double)
+        check(self.lib.wg_state_create(B.ctypes.data_as(dp), g.ctypes.data_as(dp), B.shape[0], ctypes.byref(h)))
+        self.handle = h
+        self.M = B.shape[0]
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.wg_state_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # interpreter shutdown
+            pass

@@ -103,7 +103,8 @@ struct Prepared {
   bool tile_ok;  // every term can keep its La Budde rows in dead tile columns
   double term_cost;
   std::vector<double> scales;
-  std::vector<unsigned char> ext;  // extended matrix in the kernel's scalar type
+  std::vector<unsigned char> ext;  // extended matrix in the kernel's scalar type (empty: formed on device)
+  size_t ext_bytes = 0;
 };
 
 struct Group {
@@ -132,6 +133,19 @@ struct wg_plan {
   double2* d_out = nullptr;
   unsigned int* d_counters = nullptr;
   int* d_err = nullptr;
+  bool use_graph = false;
+  cudaGraphExec_t graph_exec = nullptr;
+  long long device_bytes = 0;
+  bool async_alloc = false;
+  cudaStream_t alloc_stream = nullptr;
+};
+
+struct wg_state {
+  int M = 0;
+  wg::c64* d_B = nullptr;
+  wg::c64* d_gamma = nullptr;
+  std::vector<wg::c64> gamma;  // host copy: self-loop weights of unpaired modes
+  double alpha = 1.0;          // double-float prescale (power of two, from ||B||_inf)
 };
 
 namespace wg {
@@ -356,6 +370,7 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
   const int n = in.n, lda = n + 1;
   const size_t sb = stype_bytes(P.stype);
   P.ext.assign((size_t)(n + 3) * lda * sb, 0);
+  P.ext_bytes = P.ext.size();
   auto at = [&](int r, int c) { return P.ext.data() + ((size_t)r * lda + c) * sb; };
   double re, im;
   for (int r = 0; r < n; ++r)
@@ -391,15 +406,143 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
 }
 
 
-static int build_plan(const wg_instance* v, int count, int precision, double chunk_scale, wg_plan* pl) {
+// Device-side formation of instance pools from a resident Gaussian state (serving).
+struct GatherDev {
+  long long a_off;  // pool byte offset of the instance's extended matrix
+  int x_off;        // first index of the instance's pairing in the index array
+  int n;            // 2E
+  int oddmode;      // -1: none
+  int stype;
+  double alpha, salpha;
+};
+struct GatherSpec {
+  const c64* B = nullptr;
+  const c64* gamma = nullptr;
+  int M = 0;
+  std::vector<GatherDev> desc;
+  std::vector<int> idx;
+};
+
+static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_options& opt, wg_plan* pl,
+                         GatherSpec* gs);
+
+// One block per instance: writes [[B[x][:,x], gamma[x]], [gamma[x]^T, 0], [B[o, x], 0], [0]]
+// (alpha / sqrt(alpha) prescaled) into the instance's pool slot in its scalar type.
+static __global__ void gather_kernel(const GatherDev* __restrict__ gd, const int* __restrict__ idx,
+                                     const c64* __restrict__ B, const c64* __restrict__ gamma, int M,
+                                     unsigned char* __restrict__ pool) {
+  const GatherDev G = gd[blockIdx.x];
+  const int n = G.n, lda = n + 1;
+  const int* x = idx + G.x_off;
+  const int total = (n + 3) * lda;
+  for (int e = threadIdx.x; e < total; e += blockDim.x) {
+    const int i = e / lda, j = e % lda;
+    c64 v = {0.0, 0.0};
+    double sc = 0.0;
+    if (i < n && j < n) { v = B[(size_t)x[i] * M + x[j]]; sc = G.alpha; }
+    else if (i < n && j == n) { v = gamma[x[i]]; sc = G.salpha; }
+    else if (i == n && j < n) { v = gamma[x[j]]; sc = G.salpha; }
+    else if (i == n + 1 && j < n && G.oddmode >= 0) { v = B[(size_t)G.oddmode * M + x[j]]; sc = G.alpha; }
+    const double re = v.re * sc, im = v.im * sc;
+    unsigned char* dst = pool + G.a_off;
+    if (G.stype == ST_CPLX64) {
+      reinterpret_cast<c64*>(dst)[e] = {re, im};
+    } else {
+      const float hr = __double2float_rn(re), hi = __double2float_rn(im);
+      reinterpret_cast<cdf*>(dst)[e] = {{hr, __double2float_rn(re - (double)hr)}, {hi, __double2float_rn(im - (double)hi)}};
+    }
+  }
+}
+
+// Loop-hafnian instance of one serving request (the host part of prepare() for WG_KIND_LOOP,
+// without a host copy of the matrix).
+static int prepare_request(const wg_request& r, const wg_state& st, int precision, Prepared& P, GatherDev& g,
+                           std::vector<int>& idx) {
+  memset(&P.d, 0, sizeof(P.d));
+  InstDev& d = P.d;
+  if (r.E < 1 || r.E > MAX_EDGES || !r.x || !r.edge_reps) return fail(WG_EINVAL, "request needs 1..32 edges");
+  const bool odd = r.oddmode >= 0;
+  if (r.oddmode >= st.M) return fail(WG_EINVAL, "unpaired mode out of range");
+  long long sumr = 0, steps = 1;
+  int maxr = 0;
+  for (int i = 0; i < r.E; ++i) {
+    const long long rr = r.edge_reps[i];
+    if (rr < 0 || rr > BINOM_N - 1) return fail(WG_EINVAL, "edge repetition out of range");
+    sumr += rr;
+    maxr = std::max(maxr, (int)rr);
+  }
+  for (int i = 0; i < 2 * r.E; ++i)
+    if (r.x[i] < 0 || r.x[i] >= st.M) return fail(WG_EINVAL, "mode index out of range");
+  const double alpha = precision == WG_PREC_DF ? st.alpha : 1.0, salpha = std::sqrt(alpha);
+  d.kind = odd ? KIND_LOOP_ODD : KIND_LOOP;
+  d.n = 2 * r.E;
+  d.E = r.E;
+  d.glynn = 1;
+  d.nb = 1;
+  d.ne = odd ? 1 : 0;
+  d.lda = d.n + 1;
+  d.unit_binoms = maxr <= 1;
+  d.N = (int)(2 * sumr + (odd ? 1 : 0));
+  d.K = d.N / 2;
+  d.Nodd = odd ? d.N : 0;
+  d.nout = 1;
+  d.half_first = odd ? 0 : 1;
+  if (odd) d.oddloop = {st.gamma[r.oddmode].re * salpha, st.gamma[r.oddmode].im * salpha};
+  const int e = odd ? d.N / 2 : d.N / 2 - 1;
+  P.scales.assign(1, std::ldexp(1.0, -e) * std::pow(alpha, -0.5 * d.N));
+  for (int i = 0; i < r.E; ++i) {
+    const int R = (i == 0 && d.half_first) ? (int)(r.edge_reps[0] + 2) / 2 : (int)r.edge_reps[i] + 1;
+    d.radix[i] = R;
+    d.reps[i] = (int)r.edge_reps[i];
+    if (steps > (1LL << 62) / R) return fail(WG_EINVAL, "too many sieve terms");
+    steps *= R;
+  }
+  d.steps = steps;
+  int nnz = 0;
+  bool all_odd = true;
+  for (int i = 0; i < r.E; ++i) {
+    nnz += r.edge_reps[i] > 0;
+    all_odd = all_odd && (r.edge_reps[i] % 2 == 1);
+  }
+  P.m_max = 2 * nnz;
+  P.mb_max = P.m_max + 1;
+  P.rows_max = P.m_max + 1 + d.ne;
+  P.kc_max = std::min(d.K, P.m_max);
+  P.nser_need = std::max(std::max(d.K, d.Nodd), P.m_max) + 2;
+  P.narr = 8;
+  P.tile_ok = true;  // bordered tile
+  P.term_cost = (double)P.mb_max * P.mb_max * P.mb_max + 64.0;
+  if (P.rows_max > 80 || d.K > 250 || d.Nodd > 250) return fail(WG_EINVAL, "request too large");
+  P.stype = precision == WG_PREC_DF ? ST_CPLXDF : ST_CPLX64;
+  P.ext.clear();
+  P.ext_bytes = (size_t)(d.n + 3) * (d.n + 1) * stype_bytes(P.stype);
+  g.x_off = (int)idx.size();
+  g.n = d.n;
+  g.oddmode = r.oddmode;
+  g.stype = P.stype;
+  g.alpha = alpha;
+  g.salpha = salpha;
+  for (int i = 0; i < 2 * r.E; ++i) idx.push_back(r.x[i]);
+  return WG_OK;
+}
+
+static int build_plan(const wg_instance* v, int count, int precision, const wg_plan_options& opt, wg_plan* pl) {
   if (count < 0 || (count > 0 && !v)) return fail(WG_EINVAL, "bad instance list");
   if (precision != WG_PREC_FP64 && precision != WG_PREC_DF) return fail(WG_EINVAL, "unknown precision %d", precision);
-  if (!(chunk_scale > 0)) chunk_scale = 1.0;
   std::vector<Prepared> P(count);
   for (int i = 0; i < count; ++i) {
     int rc = prepare(v[i], precision, P[i]);
     if (rc) return fail(rc, "instance %d: %s", i, g_err.c_str());
   }
+  return finalize_plan(P, precision, opt, pl, nullptr);
+}
+
+static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_options& opt, wg_plan* pl,
+                         GatherSpec* gs) {
+  const int count = (int)P.size();
+  const double chunk_scale = opt.chunk_scale > 0 ? opt.chunk_scale : 1.0;
+  const int wpc_cap = opt.max_warps_per_cta > 0 ? std::min(opt.max_warps_per_cta, 8) : 8;
+  pl->use_graph = opt.use_graph != 0;
   pl->precision = precision;
   // outputs and scales in instance order
   int out = 0;
@@ -411,7 +554,7 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
     scales.insert(scales.end(), P[i].scales.begin(), P[i].scales.end());
   }
   pl->total_out = out;
-  // groups by (stype, ns)
+  // groups by (stype, ns); with merge_classes one group per scalar type, at the largest class
   struct GKey { int st, ns; };
   std::vector<GKey> keys;
   std::vector<int> gid(count);
@@ -420,16 +563,19 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
     if (ns < 0) return fail(WG_EINVAL, "instance %d: term matrix too large", i);
     int g = -1;
     for (size_t k = 0; k < keys.size(); ++k)
-      if (keys[k].st == P[i].stype && keys[k].ns == ns) g = (int)k;
+      if (keys[k].st == P[i].stype && (opt.merge_classes || keys[k].ns == ns)) g = (int)k;
     if (g < 0) { keys.push_back({P[i].stype, ns}); g = (int)keys.size() - 1; }
+    if (keys[g].ns < ns) keys[g].ns = ns;
     gid[i] = g;
   }
   // pool
   size_t pool_bytes = 0;
   for (int i = 0; i < count; ++i) {
     P[i].d.a_off = (long long)pool_bytes;
-    pool_bytes += (P[i].ext.size() + 255) & ~(size_t)255;
+    pool_bytes += (P[i].ext_bytes + 255) & ~(size_t)255;
   }
+  if (gs)
+    for (int i = 0; i < count; ++i) gs->desc[i].a_off = P[i].d.a_off;
   int nparts = 0;
   for (size_t g = 0; g < keys.size(); ++g) {
     Group G;
@@ -452,7 +598,7 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
       }
     G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
     const int max_smem = 227 * 1024;
-    int wpc = std::min(8, max_smem / G.L.bytes);
+    int wpc = std::min(wpc_cap, max_smem / G.L.bytes);
     if (wpc < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
     int per_sm = 0;
 #define WG_OCC(S, NS) per_sm = occupancy_one<S, NS>(wpc, wpc * G.L.bytes)
@@ -504,10 +650,17 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
   const size_t b_out = al(sizeof(double2) * std::max(out, 1));
   const size_t b_cnt = al(sizeof(unsigned int) * std::max<size_t>(pl->groups.size(), 1));
   const size_t b_err = al(sizeof(int));
-  const size_t total = b_inst + b_chunks + b_pool + b_parts + b_scales + b_out + b_cnt + b_err;
-  if (cudaMalloc(&pl->dmem, total) != cudaSuccess) {
+  const size_t b_gdesc = gs ? al(sizeof(GatherDev) * std::max<size_t>(gs->desc.size(), 1)) : 0;
+  const size_t b_gidx = gs ? al(sizeof(int) * std::max<size_t>(gs->idx.size(), 1)) : 0;
+  const size_t total = b_inst + b_chunks + b_pool + b_parts + b_scales + b_out + b_cnt + b_err + b_gdesc + b_gidx;
+  cudaStream_t cs = (cudaStream_t)opt.stream;
+  pl->alloc_stream = cs;
+  pl->async_alloc = cs != nullptr;
+  const cudaError_t ae = pl->async_alloc ? cudaMallocAsync(&pl->dmem, total, cs) : cudaMalloc(&pl->dmem, total);
+  if (ae != cudaSuccess) {
     cudaGetLastError();
-    return fail(WG_ENOMEM, "cudaMalloc of %zu bytes failed", total);
+    pl->dmem = nullptr;
+    return fail(WG_ENOMEM, "device allocation of %zu bytes failed", total);
   }
   unsigned char* base = (unsigned char*)pl->dmem;
   pl->d_inst = (InstDev*)base; base += b_inst;
@@ -517,21 +670,50 @@ static int build_plan(const wg_instance* v, int count, int precision, double chu
   pl->d_scales = (double*)base; base += b_scales;
   pl->d_out = (double2*)base; base += b_out;
   pl->d_counters = (unsigned int*)base; base += b_cnt;
-  pl->d_err = (int*)base;
+  pl->d_err = (int*)base; base += b_err;
+  pl->device_bytes = (long long)total;
   // staging: one host buffer with the same layout for the upload
   std::vector<unsigned char> host(b_inst + b_chunks + b_pool + b_parts + b_scales, 0);
   memcpy(host.data(), pl->inst.data(), sizeof(InstDev) * count);
   if (!pl->chunks.empty()) memcpy(host.data() + b_inst, pl->chunks.data(), sizeof(ChunkDev) * pl->chunks.size());
   for (int i = 0; i < count; ++i)
-    memcpy(host.data() + b_inst + b_chunks + P[i].d.a_off, P[i].ext.data(), P[i].ext.size());
+    if (!P[i].ext.empty()) memcpy(host.data() + b_inst + b_chunks + P[i].d.a_off, P[i].ext.data(), P[i].ext.size());
   if (!scales.empty()) memcpy(host.data() + b_inst + b_chunks + b_pool + b_parts, scales.data(), sizeof(double) * scales.size());
-  CK(cudaMemcpy(pl->dmem, host.data(), host.size(), cudaMemcpyHostToDevice));
-  pl->h2d_bytes = (long long)host.size();
-  CK(cudaMemset(pl->d_counters, 0, b_cnt + b_err));
+  // uploads: stream-ordered on the creation stream when one is given (pageable sources are
+  // staged before cudaMemcpyAsync returns), else synchronous
+  auto up = [&](void* dst, const void* src, size_t bytes) -> cudaError_t {
+    return cs ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, cs)
+              : cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  if (gs) {
+    // pools are formed on the device: only descriptors, chunks, scales and indices travel
+    CK(up(pl->dmem, host.data(), b_inst + b_chunks));
+    CK(up((unsigned char*)pl->dmem + b_inst + b_chunks + b_pool + b_parts,
+          host.data() + b_inst + b_chunks + b_pool + b_parts, b_scales));
+    GatherDev* d_desc = (GatherDev*)((unsigned char*)pl->d_err + b_err);
+    int* d_idx = (int*)((unsigned char*)d_desc + b_gdesc);
+    CK(up(d_desc, gs->desc.data(), sizeof(GatherDev) * gs->desc.size()));
+    if (!gs->idx.empty()) CK(up(d_idx, gs->idx.data(), sizeof(int) * gs->idx.size()));
+    if (count > 0) {
+      gather_kernel<<<count, 256, 0, cs>>>(d_desc, d_idx, gs->B, gs->gamma, gs->M, pl->d_pool);
+      CK(cudaGetLastError());
+    }
+    pl->h2d_bytes = (long long)(b_inst + b_chunks + b_scales + sizeof(GatherDev) * gs->desc.size() +
+                                sizeof(int) * gs->idx.size());
+  } else {
+    CK(up(pl->dmem, host.data(), host.size()));
+    pl->h2d_bytes = (long long)host.size();
+  }
+  if (cs) {
+    CK(cudaMemsetAsync(pl->d_counters, 0, b_cnt + b_err, cs));
+  } else {
+    CK(cudaMemset(pl->d_counters, 0, b_cnt + b_err));
+    CK(cudaStreamSynchronize(0));
+  }
   return WG_OK;
 }
 
-static int execute_plan(wg_plan* pl, cudaStream_t st) {
+static int launch_plan(wg_plan* pl, cudaStream_t st) {
   for (size_t g = 0; g < pl->groups.size(); ++g) {
     const Group& G = pl->groups[g];
     SieveParams p;
@@ -562,9 +744,40 @@ static int execute_plan(wg_plan* pl, cudaStream_t st) {
   return WG_OK;
 }
 
+// Direct launches, or -- with use_graph -- one CUDA graph captured on first use (the launch
+// attributes are set by a direct execution first) and replayed on the caller's stream.
+static int execute_plan(wg_plan* pl, cudaStream_t st) {
+  if (!pl->use_graph) return launch_plan(pl, st);
+  if (!pl->graph_exec) {
+    int rc = launch_plan(pl, st);  // sets the kernels' shared-memory attributes, warms up
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(st));
+    cudaStream_t cap;
+    CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      rc = launch_plan(pl, cap);
+      e = cudaStreamEndCapture(cap, &graph);
+    }
+    if (e == cudaSuccess && rc == 0) e = cudaGraphInstantiate(&pl->graph_exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cap);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(WG_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    return WG_OK;  // this call already executed the plan once
+  }
+  CK(cudaGraphLaunch(pl->graph_exec, st));
+  return WG_OK;
+}
+
 static void destroy_plan(wg_plan* pl) {
   if (!pl) return;
-  if (pl->dmem) cudaFree(pl->dmem);
+  if (pl->graph_exec) cudaGraphExecDestroy(pl->graph_exec);
+  if (pl->dmem) {
+    if (pl->async_alloc) cudaFreeAsync(pl->dmem, pl->alloc_stream);
+    else cudaFree(pl->dmem);
+  }
   delete pl;
 }
 
@@ -625,16 +838,28 @@ int wg_instance_outputs(const wg_instance* in) {
   return 1;
 }
 
-int wg_plan_create(const wg_instance* inst, int count, int precision, double chunk_scale, wg_plan** plan) {
+int wg_plan_create_ex(const wg_instance* inst, int count, int precision, const wg_plan_options* options,
+                      wg_plan** plan) {
   if (!plan) return fail(WG_EINVAL, "plan is NULL");
   *plan = nullptr;
   int rc = ensure_init(-1);
   if (rc) return rc;
+  wg_plan_options opt;
+  memset(&opt, 0, sizeof(opt));
+  opt.chunk_scale = 1.0;
+  if (options) opt = *options;
   wg_plan* pl = new wg_plan();
-  rc = build_plan(inst, count, precision, chunk_scale, pl);
+  rc = build_plan(inst, count, precision, opt, pl);
   if (rc) { destroy_plan(pl); return rc; }
   *plan = pl;
   return WG_OK;
+}
+
+int wg_plan_create(const wg_instance* inst, int count, int precision, double chunk_scale, wg_plan** plan) {
+  wg_plan_options opt;
+  memset(&opt, 0, sizeof(opt));
+  opt.chunk_scale = chunk_scale;
+  return wg_plan_create_ex(inst, count, precision, &opt, plan);
 }
 
 int wg_plan_execute(wg_plan* plan, void* stream) {
@@ -678,6 +903,73 @@ int wg_plan_chunk(const wg_plan* plan, int chunk, int* inst, int* part, long lon
   if (t1) *t1 = c.t1;
   return (int)plan->chunks.size();
 }
+
+int wg_state_create(const double* B, const double* gamma, int M, wg_state** state) {
+  if (!state || !B || !gamma || M < 1) return fail(WG_EINVAL, "bad state arguments");
+  *state = nullptr;
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  wg_state* st = new wg_state();
+  st->M = M;
+  st->gamma.resize(M);
+  double rs = 0;
+  for (int i = 0; i < M; ++i) {
+    st->gamma[i] = {gamma[2 * i], gamma[2 * i + 1]};
+    double s = 0;
+    for (int j = 0; j < M; ++j) s += std::hypot(B[2 * ((size_t)i * M + j)], B[2 * ((size_t)i * M + j) + 1]);
+    rs = std::max(rs, s);
+  }
+  if (rs > 0 && std::isfinite(rs)) st->alpha = std::exp2(-std::round(std::log2(rs)));
+  if (cudaMalloc(&st->d_B, sizeof(c64) * (size_t)M * M) != cudaSuccess ||
+      cudaMalloc(&st->d_gamma, sizeof(c64) * M) != cudaSuccess) {
+    cudaGetLastError();
+    if (st->d_B) cudaFree(st->d_B);
+    delete st;
+    return fail(WG_ENOMEM, "state allocation failed");
+  }
+  CK(cudaMemcpy(st->d_B, B, sizeof(c64) * (size_t)M * M, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(st->d_gamma, gamma, sizeof(c64) * M, cudaMemcpyHostToDevice));
+  *state = st;
+  return WG_OK;
+}
+
+int wg_state_destroy(wg_state* state) {
+  if (!state) return WG_OK;
+  if (state->d_B) cudaFree(state->d_B);
+  if (state->d_gamma) cudaFree(state->d_gamma);
+  delete state;
+  return WG_OK;
+}
+
+int wg_plan_create_requests(const wg_state* state, const wg_request* req, int count, int precision,
+                            const wg_plan_options* options, wg_plan** plan) {
+  if (!plan || !state || count < 0 || (count > 0 && !req)) return fail(WG_EINVAL, "bad request list");
+  *plan = nullptr;
+  if (precision != WG_PREC_FP64 && precision != WG_PREC_DF) return fail(WG_EINVAL, "unknown precision %d", precision);
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  wg_plan_options opt;
+  memset(&opt, 0, sizeof(opt));
+  opt.chunk_scale = 1.0;
+  if (options) opt = *options;
+  std::vector<Prepared> P(count);
+  GatherSpec gs;
+  gs.B = state->d_B;
+  gs.gamma = state->d_gamma;
+  gs.M = state->M;
+  gs.desc.resize(count);
+  for (int i = 0; i < count; ++i) {
+    rc = prepare_request(req[i], *state, precision, P[i], gs.desc[i], gs.idx);
+    if (rc) return fail(rc, "request %d: %s", i, g_err.c_str());
+  }
+  wg_plan* pl = new wg_plan();
+  rc = finalize_plan(P, precision, opt, pl, &gs);
+  if (rc) { destroy_plan(pl); return rc; }
+  *plan = pl;
+  return WG_OK;
+}
+
+long long wg_plan_device_bytes(const wg_plan* plan) { return plan ? plan->device_bytes : 0; }
 
 int wg_plan_transfer_bytes(const wg_plan* plan, long long* h2d, long long* d2h) {
   if (!plan) return fail(WG_EINVAL, "plan is NULL");
