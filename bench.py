@@ -267,6 +267,167 @@ def run_gpu(args, rank, world, local):
     plan.close()
 
 
+def _gpu_setup(local=0):
+    import torch
+
+    torch.cuda.set_device(local)
+    from thewalrus_gb300 import _native as nat
+
+    nat.check(nat.load().wg_init(local))
+    return torch, nat
+
+
+def run_loop(args):
+    """Loop hafnian of the 20-mode Gaussian-state reduced matrix (40 photons, repeats <= 3):
+    hafnian_repeated(A, rpt, mu=gamma, loop=True), device time per call and end to end."""
+    import numpy as np
+
+    torch, nat = _gpu_setup()
+    import thewalrus_gb300 as tw
+    from thewalrus_gb300 import costmodel, workloads as wl
+
+    A, gamma, rpt = wl.gaussian_state_loop(modes=20, seed=1, photons=40, max_rep=3)
+    inst = tw.prepare_loop_hafnian(A, gamma, list(rpt))
+    plan = nat.Plan([inst], precision=args.precision)
+    s = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        plan.execute(s.cuda_stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.steps):
+        plan.execute(s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    dev_s = e0.elapsed_time(e1) / 1e3 / args.steps
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        val = tw.hafnian_repeated(A, list(rpt), mu=gamma, loop=True, precision=args.precision)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    x, reps, odd = tw.matched_reps(list(rpt))
+    flops = costmodel.instance_flops(reps, True, kind="loop", odd=odd is not None)
+    print(json.dumps({"metric": "loop hafnians/s (20-mode Gaussian state, 40 photons)", "value": 1 / dev_s,
+                      "unit": "hafnians/s", "ms_per_step": dev_s * 1e3, "e2e": {"value": 1 / e2e_s, "unit": "hafnians/s"},
+                      "edge_reps": [int(r) for r in reps], "terms": int(np.prod([r + 1 for r in reps]) // 1),
+                      "achieved_tflops": flops / dev_s / 1e12, "precision": args.precision,
+                      "result": [float(val.real), float(val.imag)]}), flush=True)
+
+
+def run_batch(args):
+    """4096 hafnians of uneven even n in {8..40} (half real non-negative, half complex) plus 16
+    loop_hafnian_batch calls (12 modes, cutoff 6) in one autotuned, graph-replayed plan, against
+    per-call launches of the same instances (a bounded sample of them)."""
+    import numpy as np
+
+    torch, nat = _gpu_setup()
+    import thewalrus_gb300 as tw
+    from thewalrus_gb300 import autotune, workloads as wl
+
+    count = args.batch_count
+    mats = wl.batch_instances(count=count, seed=2)
+    calls = wl.batch_loop_calls(count=16, seed=3, modes=12, cutoff=6)
+    insts = [tw.prepare_hafnian(A) for A in mats] + \
+        [tw.prepare_loop_hafnian_batch(B, D, list(f), c) for B, D, f, c in calls]
+    sub = insts[::16]
+    cands = [{"chunk_scale": cs, "max_warps_per_cta": 0, "merge_classes": mc}
+             for cs in (0.5, 1.0, 2.0) for mc in (False, True)]
+    best, table = autotune.tune(sub, precision=args.precision, candidates=cands, repeats=1, use_cache=False)
+    plan = nat.Plan(insts, precision=args.precision, use_graph=True, **best)
+    s = torch.cuda.current_stream()
+    plan.execute(s.cuda_stream)  # first execution captures the graph
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    plan.execute(s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    batched_s = e0.elapsed_time(e1) / 1e3
+    got = plan.read(s.cuda_stream)
+    # per-call plain launches on a deterministic sample (every 32nd instance), same accuracy
+    sample = list(range(0, len(mats), 32))
+    t0 = time.perf_counter()
+    per = [tw.hafnian(mats[i], precision=args.precision) for i in sample]
+    per_call_s = time.perf_counter() - t0
+    idx_sum = 0
+    err = 0.0
+    for k, i in enumerate(sample):
+        err = max(err, abs(per[k] - got[i]) / abs(per[k]))
+        idx_sum += 1
+    # the batched cost of the same sample, in proportion of its flops
+    from thewalrus_gb300 import costmodel
+    fl = [costmodel.plain_hafnian_flops(A.shape[0], np.iscomplexobj(A)) for A in mats]
+    frac = sum(fl[i] for i in sample) / sum(fl)
+    outputs = len(mats) + 16
+    print(json.dumps({
+        "metric": "batched hafnians/s (4096 uneven n in 8..40 + 16 loop_hafnian_batch, one plan)",
+        "value": outputs / batched_s, "unit": "hafnians/s", "seconds": batched_s,
+        "per_call": {"hafnians_per_s": len(sample) / per_call_s, "sample": len(sample),
+                     "batched_equivalent_hafnians_per_s": len(sample) / (batched_s * frac)},
+        "max_rel_diff_batched_vs_per_call": err, "autotuned": best,
+        "autotune_table": [[c, t] for c, t in table], "kernel_launches": plan.kernel_launches,
+        "graph": True, "precision": args.precision}), flush=True)
+
+
+def run_serve(args):
+    """Poisson streams of probability requests on 64-mode synthetic pure Gaussian states; rates
+    swept; p50/p99 latency and hafnians/s per rate."""
+    _gpu_setup()
+    from thewalrus_gb300.serving import GaussianState, ProbabilityServer, poisson_requests, summary
+
+    states = [GaussianState.synthetic(modes=64, seed=s) for s in range(4)]
+    srv = ProbabilityServer(states, precision=args.precision, max_batch=256, streams=3)
+    lo, hi = args.photons
+    srv.serve(poisson_requests(states, 1e6, 8, photons=(lo, min(hi, lo + 8)), seed=99))  # warm-up
+    rows = []
+    for rate in args.rates:
+        reqs = poisson_requests(states, rate, args.serve_count, photons=(lo, hi), seed=int(rate))
+        t0 = time.perf_counter()
+        res = srv.serve(reqs)
+        span = time.perf_counter() - t0
+        sm = summary(res, makespan=span)
+        sm["rate"] = rate
+        rows.append(sm)
+    print(json.dumps({"metric": "served loop-hafnian probabilities (64-mode states, %d-%d photons)" % (lo, hi),
+                      "unit": "hafnians/s", "precision": args.precision, "sweep": rows}), flush=True)
+
+
+def run_precision(args):
+    """Relative error of FP64 and double-float sieve terms against the _Float128 oracle (n <= 24)
+    and exact integer rounding for 0/1 adjacency matrices; the n=48 classes are timed."""
+    import numpy as np
+
+    torch, nat = _gpu_setup()
+    import oracle
+    import thewalrus_gb300 as tw
+    from thewalrus_gb300 import workloads as wl
+
+    gens = {"complex": wl.complex_symmetric, "real_signed": wl.real_signed, "real_nonneg": wl.real_nonneg,
+            "adjacency01": wl.adjacency01}
+    table = {}
+    for name, gen in gens.items():
+        errs = {"fp64": [], "df": []}
+        for seed in range(args.precision_seeds):
+            A = gen(args.precision_n, seed=seed)
+            ref = complex(oracle.hafnian(A, precision="quad"))
+            for p in ("fp64", "df"):
+                g = tw.hafnian(A, precision=p)
+                errs[p].append(abs(g - ref) / abs(ref) if ref != 0 else abs(g))
+                if name == "adjacency01" and p == "fp64":
+                    assert round(g.real) == round(ref.real)
+        table[name] = {p: {"max": float(np.max(v)), "median": float(np.median(v))} for p, v in errs.items()}
+    timing = {}
+    for name, gen in gens.items():
+        A = gen(48, seed=0)
+        for p in ("fp64", "df"):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            tw.hafnian(A, precision=p)
+            timing["%s/%s" % (name, p)] = time.perf_counter() - t0
+    print(json.dumps({"metric": "relative error vs _Float128 oracle (n=%d, %d seeds per class)"
+                      % (args.precision_n, args.precision_seeds), "errors": table,
+                      "n48_seconds_per_hafnian": timing}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -277,10 +438,22 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["n40", "loop", "batch", "serve", "precision"], default="n40",
+                    help="n40: the benchmark line; the others report the other configurations")
+    ap.add_argument("--batch-count", type=int, default=4096)
+    ap.add_argument("--rates", type=float, nargs="+", default=[100.0, 1000.0, 5000.0, 20000.0])
+    ap.add_argument("--serve-count", type=int, default=64)
+    ap.add_argument("--photons", type=int, nargs=2, default=[8, 44])
+    ap.add_argument("--precision-n", type=int, default=20)
+    ap.add_argument("--precision-seeds", type=int, default=8)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload != "n40":
+        if rank == 0:
+            {"loop": run_loop, "batch": run_batch, "serve": run_serve, "precision": run_precision}[args.workload](args)
         return
     run_gpu(args, rank, world, local)
 

@@ -32,6 +32,21 @@ __device__ __forceinline__ unsigned long long absbits_d(double x) {
 }
 __device__ __forceinline__ unsigned int absbits_f(float x) { return (unsigned)__float_as_int(x) & 0x7fffffffu; }
 
+// 1/x for the pivots: the PTX approximate reciprocal (rcp.approx.ftz.f64) refined by two Newton
+// steps r <- r + r(1 - x r), which square the relative error each time; inputs whose exponent
+// leaves the approximation's safe range take the IEEE division instead.
+__device__ __forceinline__ double recip_newton(double x) {
+  const unsigned hi = (unsigned)(__double_as_longlong(x) >> 32);
+  const unsigned ex = (hi >> 20) & 0x7ffu;
+  if (ex < 64u || ex > 2000u) return 1.0 / x;
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = ::fma(-x, r, 1.0);
+  r = ::fma(r, e, r);
+  e = ::fma(-x, r, 1.0);
+  return ::fma(r, e, r);
+}
+
 // ---------------------------------------------------------------- double-float primitives
 __device__ __forceinline__ dfr df_two_sum(float a, float b) {
   float s = a + b;
@@ -114,7 +129,7 @@ struct Ar<double> {
   __device__ static __forceinline__ c64 to_c64(S a) { return {a, 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a); }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a) == 0; }
-  __device__ static __forceinline__ S recip(S a) { return 1.0 / a; }
+  __device__ static __forceinline__ S recip(S a) { return recip_newton(a); }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
   __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) { a = v; }
   __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return a + b; }
@@ -155,7 +170,7 @@ struct Ar<c64> {
   }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re) | absbits_d(a.im)) == 0; }
   __device__ static __forceinline__ S recip(S a) {
-    double d = 1.0 / ::fma(a.re, a.re, a.im * a.im);
+    const double d = recip_newton(::fma(a.re, a.re, a.im * a.im));
     return {a.re * d, neg_d(a.im) * d};
   }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return i ? a.im : a.re; }

@@ -43,9 +43,9 @@ static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int ns
   L.tilewin = tilewin ? 1 : 0;
   off += al((tilewin ? 3 : L.kw) * L.kw * sb);
   L.off_tb = off;
-  off += al(L.kw * sb);
+  off += al(2 * L.kw * sb);  // T_r of two rows
   L.off_part = off;
-  off += al(64 * sb);
+  off += al(96 * sb);  // La Budde piece partials (3 per lane)
   L.off_ser = off;
   off += al(narr * L.nser * sb);
   L.off_int = off;
@@ -114,6 +114,70 @@ static inline bool lb_schedule(int Ki, LbLane* lanes, LbOwner* own) {
     if (fits) return true;
     for (int j = 0; j <= LB_KMAX; ++j) own[j] = LbOwner{0, {0, 0, 0, 0, 0, 0, 0}};
     for (int l = 0; l < 32; ++l) lanes[l] = LbLane{0, 0, 0, 0, 0, 0, 0, 0};
+  }
+  return false;
+}
+
+// Two-row steady-state schedule for K coefficients: the pieces of both rows' r-sums (each j's
+// j-1 products cut into ceil((j-1)/t) runs, per row) packed into 32 lanes, at most three pieces
+// per lane, largest first onto the least-loaded lane that fits; smallest feasible t.
+static inline bool lb_schedule2(int K, LbLane2* lanes, LbOwner2* own) {
+  for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
+  for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
+  const int W = K * (K - 1) / 2;
+  if (W == 0) return true;
+  struct Piece { int row, j, rlo, len; };
+  for (int t = std::max(1, (2 * W + 31) / 32); t <= 64; ++t) {
+    int npcs = 0;
+    for (int j = 2; j <= K; ++j) npcs += 2 * ((j - 1 + t - 1) / t);
+    if (npcs > 96) continue;
+    Piece pcs[96];
+    npcs = 0;
+    for (int row = 0; row < 2; ++row)
+      for (int j = 2; j <= K; ++j) {
+        const int x = j - 1, p = (x + t - 1) / t;
+        int r = 1;
+        for (int q = 0; q < p; ++q) {
+          const int len = x / p + (q < x % p ? 1 : 0);
+          pcs[npcs++] = {row, j, r, len};
+          r += len;
+        }
+      }
+    for (int a = 1; a < npcs; ++a) {  // stable insertion sort, longest first
+      const Piece key = pcs[a];
+      int b = a - 1;
+      while (b >= 0 && pcs[b].len < key.len) { pcs[b + 1] = pcs[b]; --b; }
+      pcs[b + 1] = key;
+    }
+    int load[32] = {0}, nseg[32] = {0};
+    Piece seg[32][3];
+    bool ok = true;
+    for (int q = 0; q < npcs && ok; ++q) {
+      int best = -1;
+      for (int l = 0; l < 32; ++l)
+        if (nseg[l] < 3 && load[l] + pcs[q].len <= t && (best < 0 || load[l] < load[best])) best = l;
+      if (best < 0) ok = false;
+      else { seg[best][nseg[best]++] = pcs[q]; load[best] += pcs[q].len; }
+    }
+    if (!ok) continue;
+    bool fits = true;
+    for (int l = 0; l < 32 && fits; ++l) {
+      LbLane2& L = lanes[l];
+      for (int k = 0; k < nseg[l]; ++k) {
+        L.j[k] = (signed char)seg[l][k].j;
+        L.rlo[k] = (signed char)seg[l][k].rlo;
+        L.len[k] = (signed char)seg[l][k].len;
+        if (seg[l][k].row) L.rowmask |= (unsigned char)(1u << k);
+        LbOwner2& o = own[seg[l][k].j];
+        unsigned char& n = seg[l][k].row ? o.n1 : o.n0;
+        unsigned char* sl = seg[l][k].row ? o.s1 : o.s0;
+        if (n >= 7) { fits = false; break; }
+        sl[n++] = (unsigned char)(3 * l + k);
+      }
+    }
+    if (fits) return true;
+    for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
+    for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
   }
   return false;
 }

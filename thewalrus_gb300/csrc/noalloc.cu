@@ -43,6 +43,8 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 static __device__ LbLane g_lane_tab[(LB_KMAX + 1) * 32];
 static __device__ LbOwner g_own_tab[(LB_KMAX + 1) * (LB_KMAX + 1)];
+static __device__ LbLane2 g_lane2_tab[(LB2_KMAX + 1) * 32];
+static __device__ LbOwner2 g_own2_tab[(LB2_KMAX + 1) * (LB2_KMAX + 1)];
 
 // byte offsets inside g_scratch
 constexpr size_t kOffInst = 0;
@@ -57,6 +59,8 @@ struct DeviceState {
   unsigned char* scratch = nullptr;  // device address of g_scratch
   LbLane* lanes = nullptr;
   LbOwner* own = nullptr;
+  LbLane2* lanes2 = nullptr;
+  LbOwner2* own2 = nullptr;
   int sms = 0;
 };
 static DeviceState g_dev[kMaxDevices];
@@ -80,6 +84,10 @@ static int setup(int dev, DeviceState** out) {
     s.lanes = (LbLane*)p;
     if (cudaGetSymbolAddress(&p, g_own_tab) != cudaSuccess) return err(WG_ECUDA, "cudaGetSymbolAddress(owner table) failed");
     s.own = (LbOwner*)p;
+    if (cudaGetSymbolAddress(&p, g_lane2_tab) != cudaSuccess) return err(WG_ECUDA, "cudaGetSymbolAddress(lane2 table) failed");
+    s.lanes2 = (LbLane2*)p;
+    if (cudaGetSymbolAddress(&p, g_own2_tab) != cudaSuccess) return err(WG_ECUDA, "cudaGetSymbolAddress(owner2 table) failed");
+    s.own2 = (LbOwner2*)p;
     static double binom[BINOM_N][BINOM_N];
     for (int i = 0; i < BINOM_N; ++i)
       for (int j = 0; j < BINOM_N; ++j) {
@@ -94,10 +102,16 @@ static int setup(int dev, DeviceState** out) {
     static LbOwner own[(LB_KMAX + 1) * (LB_KMAX + 1)];
     for (int k = 0; k <= LB_KMAX; ++k)
       if (!lb_schedule(k, &lanes[k * 32], &own[k * (LB_KMAX + 1)])) return err(WG_EINVAL, "no La Budde schedule");
+    static LbLane2 lanes2[(LB2_KMAX + 1) * 32];
+    static LbOwner2 own2[(LB2_KMAX + 1) * (LB2_KMAX + 1)];
+    for (int k = 0; k <= LB2_KMAX; ++k)
+      if (!lb_schedule2(k, &lanes2[k * 32], &own2[k * (LB2_KMAX + 1)])) return err(WG_EINVAL, "no La Budde schedule");
     if (cudaMemcpyToSymbol(c_binom, binom, sizeof(binom)) != cudaSuccess ||
         cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)) != cudaSuccess ||
         cudaMemcpyToSymbol(g_lane_tab, lanes, sizeof(lanes)) != cudaSuccess ||
-        cudaMemcpyToSymbol(g_own_tab, own, sizeof(own)) != cudaSuccess)
+        cudaMemcpyToSymbol(g_own_tab, own, sizeof(own)) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_lane2_tab, lanes2, sizeof(lanes2)) != cudaSuccess ||
+        cudaMemcpyToSymbol(g_own2_tab, own2, sizeof(own2)) != cudaSuccess)
       return err(WG_ECUDA, "uploading the constant tables failed");
     if (cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       return err(WG_ECUDA, "cudaDeviceGetAttribute failed");
@@ -241,6 +255,8 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   SieveParams p;
   p.lb_lane = ds->lanes;
   p.lb_own = ds->own;
+  p.lb_lane2 = ds->lanes2;
+  p.lb_own2 = ds->own2;
   p.inst = reinterpret_cast<const InstDev*>(scr + kOffInst);
   p.chunks = reinterpret_cast<const ChunkDev*>(scr + kOffChunks);
   p.nchunks = (int)nch;

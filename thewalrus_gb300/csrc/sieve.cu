@@ -29,6 +29,8 @@ static int g_device = -1;
 static int g_num_sms = 0;
 static LbLane* g_lb_lane = nullptr;
 static LbOwner* g_lb_own = nullptr;
+static LbLane2* g_lb_lane2 = nullptr;
+static LbOwner2* g_lb_own2 = nullptr;
 
 static std::mutex g_init_mu;
 
@@ -91,6 +93,17 @@ static int ensure_init(int device) {
   }
   CK(cudaMemcpy(g_lb_lane, lanes.data(), sizeof(LbLane) * lanes.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(g_lb_own, own.data(), sizeof(LbOwner) * own.size(), cudaMemcpyHostToDevice));
+  std::vector<LbLane2> lanes2((LB2_KMAX + 1) * 32);
+  std::vector<LbOwner2> own2((LB2_KMAX + 1) * (LB2_KMAX + 1));
+  for (int k = 0; k <= LB2_KMAX; ++k)
+    if (!lb_schedule2(k, &lanes2[k * 32], &own2[k * (LB2_KMAX + 1)]))
+      return fail(WG_EINVAL, "no two-row La Budde schedule for %d coefficients", k);
+  if (!g_lb_lane2) {
+    CK(cudaMalloc(&g_lb_lane2, sizeof(LbLane2) * lanes2.size()));
+    CK(cudaMalloc(&g_lb_own2, sizeof(LbOwner2) * own2.size()));
+  }
+  CK(cudaMemcpy(g_lb_lane2, lanes2.data(), sizeof(LbLane2) * lanes2.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(g_lb_own2, own2.data(), sizeof(LbOwner2) * own2.size(), cudaMemcpyHostToDevice));
   g_device = dev;
   return WG_OK;
 }
@@ -719,6 +732,8 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
     SieveParams p;
     p.lb_lane = g_lb_lane;
     p.lb_own = g_lb_own;
+    p.lb_lane2 = g_lb_lane2;
+    p.lb_own2 = g_lb_own2;
     p.inst = pl->d_inst;
     p.chunks = pl->d_chunks + G.chunk_begin;
     p.nchunks = G.chunk_count;

@@ -84,9 +84,24 @@ struct LbOwner {
 };
 constexpr int LB_KMAX = 64;
 
+// Two-row schedule (steady state, both rows with Kc coefficients, Kc <= 32): the r-sums of rows
+// i and i+1 share one pass; up to three pieces per lane, piece q of lane l in slot 3*l+q, and
+// bit q of rowmask tells which of the two rows it belongs to.
+struct LbLane2 {
+  signed char j[3], rlo[3], len[3];
+  unsigned char rowmask;
+  unsigned char pad[2];
+};
+struct LbOwner2 {
+  unsigned char n0, n1, s0[7], s1[7];
+};
+constexpr int LB2_KMAX = 32;
+
 struct SieveParams {
   const LbLane* lb_lane;    // [(LB_KMAX+1) * 32]
   const LbOwner* lb_own;    // [(LB_KMAX+1) * (LB_KMAX+1)]
+  const LbLane2* lb_lane2;  // [(LB2_KMAX+1) * 32]
+  const LbOwner2* lb_own2;  // [(LB2_KMAX+1) * (LB2_KMAX+1)]
   const InstDev* inst;
   const ChunkDev* chunks;
   int nchunks;
@@ -305,7 +320,8 @@ __device__ __forceinline__ S& cw_at(S* W, int ldw, int nb, S* win, int kw, bool 
 template <class S>
 __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __restrict__ win, int kw, bool tile,
                         S* __restrict__ bet, S* __restrict__ tb, S* __restrict__ part, S* __restrict__ cpoly,
-                        const LbLane* __restrict__ lbl, const LbOwner* __restrict__ lbo) {
+                        const LbLane* __restrict__ lbl, const LbOwner* __restrict__ lbo,
+                        const LbLane2* __restrict__ lbl2, const LbOwner2* __restrict__ lbo2) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
   for (int k = lane + 2; k <= m; k += 32) bet[k] = W[(nb + k - 1) * ldw + nb + k - 2];
@@ -316,14 +332,15 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
   // subdiagonal products P(i, r) = beta_i ... beta_{i-r+1} for r = lane+1 and lane+33, kept in
   // registers across rows: P(i, r) = beta_i * P(i-1, r-1), P(i, 1) = beta_i
   S pr0 = A::zero(), pr1 = A::zero();
-  for (int i = 1; i <= m; ++i) {
+  // T_r of row i into tbr[1..R]; returns the last usable r
+  auto fill_tb = [&](int i, S* tbr) -> int {
     const int wi = nb + i - 1;
-    const int R = (i - 1) < (Kc - 1) ? (i - 1) : (Kc - 1);  // T_r needed for r = 1..R
+    const int R = (i - 1) < (Kc - 1) ? (i - 1) : (Kc - 1);
     int rcap = R;
     if constexpr (A::fp64) {
       if (i >= 2 && A::is_zero(bet[i])) zlast = i;
       rcap = (i - zlast) < R ? (i - zlast) : R;
-      for (int r = lane + 1; r <= rcap; r += 32) tb[r] = W[(wi - r) * ldw + wi];
+      for (int r = lane + 1; r <= rcap; r += 32) tbr[r] = W[(wi - r) * ldw + wi];
     } else {
       const S bi = i >= 2 ? bet[i] : A::zero();
       const S up0 = shfl_up_s(pr0, 1);  // P(i-1, r-1) for r = lane+1
@@ -333,9 +350,75 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
       const S prev1 = lane == 0 ? last0 : up1;
       pr0 = A::mul(bi, prev0);
       pr1 = A::mul(bi, prev1);
-      if (lane + 1 <= R) tb[lane + 1] = A::mul(W[(wi - lane - 1) * ldw + wi], pr0);
-      if (lane + 33 <= R) tb[lane + 33] = A::mul(W[(wi - lane - 33) * ldw + wi], pr1);
+      if (lane + 1 <= R) tbr[lane + 1] = A::mul(W[(wi - lane - 1) * ldw + wi], pr0);
+      if (lane + 33 <= R) tbr[lane + 33] = A::mul(W[(wi - lane - 33) * ldw + wi], pr1);
     }
+    return rcap;
+  };
+  for (int i = 1; i <= m;) {
+    if (Kc >= 2 && Kc <= LB2_KMAX && i >= Kc && i + 1 <= m) {
+      // ---- rows i and i+1 together: both r-sums need rows <= i-1 only
+      const int rc0 = fill_tb(i, tb);
+      const int rc1 = fill_tb(i + 1, tb + kw);
+      __syncwarp();
+      const int wi = nb + i - 1;
+      const S alpha0 = W[wi * ldw + wi], alpha1 = W[(wi + 1) * ldw + wi + 1];
+      const int c0 = prow + 1 == kw ? 0 : prow + 1;  // circular slots of rows i and i+1
+      const int c1 = c0 + 1 == kw ? 0 : c0 + 1;
+      {
+        const LbLane2 sc = lbl2[Kc * 32 + lane];
+        const int l0 = sc.len[0], l1 = sc.len[1], l2 = sc.len[2];
+        const int tot = l0 + l1 + l2;
+        S acc = A::zero();
+        for (int it = 0; it < tot; ++it) {
+          const int q = (it >= l0) + (it >= l0 + l1);
+          const int start = q == 0 ? 0 : (q == 1 ? l0 : l0 + l1);
+          if (it == start && it > 0) {
+            part[3 * lane + q - 1] = acc;
+            acc = A::zero();
+          }
+          const int row = (sc.rowmask >> q) & 1;
+          const int j = q == 0 ? sc.j[0] : (q == 1 ? sc.j[1] : sc.j[2]);
+          const int r = (q == 0 ? sc.rlo[0] : (q == 1 ? sc.rlo[1] : sc.rlo[2])) + (it - start);
+          if (r <= (row ? rc1 : rc0)) {
+            int slot = prow + row - r;  // circular slot of row i+row-r-1
+            if (slot < 0) slot += kw;
+            const S cv = cw_at(W, ldw, nb, win, kw, tile, i + row - r - 1, slot, j - r - 1);
+            acc = A::fma(tb[row * kw + r], cv, acc);
+          }
+        }
+        if (tot > 0) part[3 * lane + (l2 > 0 ? 2 : (l1 > 0 ? 1 : 0))] = acc;
+      }
+      __syncwarp();
+      const int jj = lane + 1;
+      const LbOwner2* ow = &lbo2[Kc * (LB2_KMAX + 1) + (jj <= Kc ? jj : 0)];
+      S ci = A::zero();
+      if (jj <= Kc) {
+        S val = (jj <= i - 1) ? cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj) : A::zero();
+        val = A::fnma(alpha0, cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj - 1), val);
+        for (int k = 0; k < ow->n0; ++k) val = A::sub(val, part[ow->s0[k]]);
+        ci = val;
+      }
+      S cim1 = shfl_up_s(ci, 1);  // c[i][jj-1]
+      if (lane == 0) cim1 = A::one();
+      if (jj <= Kc) {
+        S v1 = A::fnma(alpha1, cim1, ci);
+        for (int k = 0; k < ow->n1; ++k) v1 = A::sub(v1, part[ow->s1[k]]);
+        cw_at(W, ldw, nb, win, kw, tile, i, c0, jj) = ci;
+        cw_at(W, ldw, nb, win, kw, tile, i + 1, c1, jj) = v1;
+      }
+      if (lane == 0) {
+        cw_at(W, ldw, nb, win, kw, tile, i, c0, 0) = A::one();
+        cw_at(W, ldw, nb, win, kw, tile, i + 1, c1, 0) = A::one();
+      }
+      prow = c1;
+      __syncwarp();
+      i += 2;
+      continue;
+    }
+    // ---- one row
+    const int wi = nb + i - 1;
+    const int rcap = fill_tb(i, tb);
     __syncwarp();
     const S alpha = W[wi * ldw + wi];
     const int Ki = i < Kc ? i : Kc;
@@ -370,13 +453,14 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
     for (int jj = lane + 1; jj <= Ki; jj += 32) {
       S val = (jj <= i - 1) ? cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj) : A::zero();
       val = A::fnma(alpha, cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj - 1), val);
-      const LbOwner ow = lbo[Ki * (LB_KMAX + 1) + jj];
-      for (int k = 0; k < ow.n; ++k) val = A::sub(val, part[ow.s[k]]);
+      const LbOwner* ow = &lbo[Ki * (LB_KMAX + 1) + jj];
+      for (int k = 0; k < ow->n; ++k) val = A::sub(val, part[ow->s[k]]);
       cw_at(W, ldw, nb, win, kw, tile, i, crow, jj) = val;
     }
     if (lane == 0) cw_at(W, ldw, nb, win, kw, tile, i, crow, 0) = A::one();
     prow = crow;
     __syncwarp();
+    ++i;
   }
   for (int jj = lane; jj <= Kc; jj += 32) cpoly[jj] = cw_at(W, ldw, nb, win, kw, tile, m, prow, jj);
   __syncwarp();
@@ -596,7 +680,8 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       if (kind != KIND_PLAIN) loop_krylov<S>(W, ldw, m, mb, ne, I.K, xv, eser, lam, mu, mu0);
       // characteristic polynomial coefficients of the block (xv caches the subdiagonal)
       const int Kc = I.K < m ? I.K : m;
-      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, L.tilewin != 0, xv, tb, lbpart, cpoly, P.lb_lane, P.lb_own);
+      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, L.tilewin != 0, xv, tb, lbpart, cpoly, P.lb_lane, P.lb_own,
+                 P.lb_lane2, P.lb_own2);
       const int Gdeg = I.K;  // degree of det^(-1/2) needed
       inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
 
