@@ -19,6 +19,7 @@ cpu_baseline : the CPU oracle (a C restatement of the reference algorithm: mixed
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -358,6 +359,22 @@ def run_batch(args):
     fl = [costmodel.plain_hafnian_flops(A.shape[0], np.iscomplexobj(A)) for A in mats]
     frac = sum(fl[i] for i in sample) / sum(fl)
     outputs = len(mats) + 16
+    # contrast: many small instances (n in 8..20), where per-call launch and host overheads dominate
+    small = wl.batch_instances(count=count, seed=4, n_min=8, n_max=20)
+    splan = nat.Plan([tw.prepare_hafnian(A) for A in small], precision=args.precision, use_graph=True)
+    splan.execute(s.cuda_stream)
+    torch.cuda.synchronize()
+    e0.record(s)
+    splan.execute(s.cuda_stream)
+    e1.record(s)
+    torch.cuda.synchronize()
+    small_batched_s = e0.elapsed_time(e1) / 1e3
+    sgot = splan.read(s.cuda_stream)
+    ssample = list(range(0, len(small), 16))
+    t0 = time.perf_counter()
+    sper = [tw.hafnian(small[i], precision=args.precision) for i in ssample]
+    small_per_call_s = (time.perf_counter() - t0) / len(ssample)
+    small_err = max(abs(sper[k] - sgot[i]) / abs(sper[k]) for k, i in enumerate(ssample))
     print(json.dumps({
         "metric": "batched hafnians/s (4096 uneven n in 8..40 + 16 loop_hafnian_batch, one plan)",
         "value": outputs / batched_s, "unit": "hafnians/s", "seconds": batched_s,
@@ -365,7 +382,10 @@ def run_batch(args):
                      "batched_equivalent_hafnians_per_s": len(sample) / (batched_s * frac)},
         "max_rel_diff_batched_vs_per_call": err, "autotuned": best,
         "autotune_table": [[c, t] for c, t in table], "kernel_launches": plan.kernel_launches,
-        "graph": True, "precision": args.precision}), flush=True)
+        "graph": True, "precision": args.precision,
+        "small_n": {"instances": len(small), "n_range": [8, 20], "batched_hafnians_per_s": len(small) / small_batched_s,
+                    "per_call_hafnians_per_s": 1.0 / small_per_call_s, "per_call_sample": len(ssample),
+                    "max_rel_diff_batched_vs_per_call": small_err}}), flush=True)
 
 
 def run_serve(args):
@@ -428,6 +448,64 @@ def run_precision(args):
                       "n48_seconds_per_hafnian": timing}), flush=True)
 
 
+def run_sample(args):
+    """Gaussian boson sampling by the chain rule on a synthetic 12-mode squeezed, displaced, lossy
+    state: photon-number samples/s with all attempts in lockstep (one plan per mode), the same
+    sampler one attempt at a time, threshold (click) samples/s, and the same chain on the CPU
+    oracle for a bounded number of attempts."""
+    import numpy as np
+
+    _gpu_setup()
+    from thewalrus_gb300 import samples as smp, workloads as wl
+
+    M, cutoff = args.sample_modes, 5
+    cov, mean = wl.gaussian_state_cov(M, seed=21)
+    smp.hafnian_sample_state(cov, 4, mean=mean, cutoff=cutoff)  # warm-up
+    np.random.seed(1)
+    t0 = time.perf_counter()
+    got = smp.hafnian_sample_state(cov, args.samples, mean=mean, cutoff=cutoff)
+    lock_s = time.perf_counter() - t0
+    photons = float(np.mean(np.sum(got, axis=1)))
+    np.random.seed(2)
+    seq = 16
+    t0 = time.perf_counter()
+    for _ in range(seq):
+        smp.generate_hafnian_sample(cov, mean=mean, cutoff=cutoff, max_photons=30)
+    seq_s = (time.perf_counter() - t0) / seq
+    np.random.seed(3)
+    t0 = time.perf_counter()
+    thr = 16
+    smp.torontonian_sample_state(cov, thr, mu=mean)
+    thr_s = (time.perf_counter() - t0) / thr
+    # CPU: the same chain with the oracle's loop_hafnian_batch, one attempt at a time
+    import oracle
+    chain = smp._Chain(cov, mean, 2)
+    fac = np.array([math.factorial(k) for k in range(cutoff + 1)], dtype=float)
+    np.random.seed(4)
+    t0 = time.perf_counter()
+    cpu_n = 0
+    while time.perf_counter() - t0 < args.cpu_seconds:
+        n_pure, n_het, u = chain.attempt_draws()
+        het, gam = chain.start(n_pure, n_het)
+        det = np.zeros(M, dtype=int)
+        for mode in range(M):
+            gam = gam - het[mode] * chain.B[:, mode]
+            l = oracle.loop_hafnian_batch(chain.B[:mode + 1, :mode + 1], gam[:mode + 1], det[:mode], cutoff)
+            p = (l * l.conj()).real / fac
+            det[mode] = smp._choose(p / p.sum(), u[mode])
+        cpu_n += 1
+    cpu_s = (time.perf_counter() - t0) / cpu_n
+    print(json.dumps({"metric": "GBS photon-number samples/s (%d-mode Gaussian state, cutoff %d)" % (M, cutoff),
+                      "value": args.samples / lock_s, "unit": "samples/s", "samples": args.samples,
+                      "mean_photons_per_sample": photons,
+                      "one_attempt_at_a_time_samples_per_s": 1 / seq_s,
+                      "threshold_samples_per_s": 1 / thr_s,
+                      "cpu_baseline": {"value": 1 / cpu_s, "unit": "attempts/s", "kind": "port",
+                                       "cores": int(os.environ.get("ORACLE_THREADS", os.cpu_count() or 1)),
+                                       "sample": "%d attempts, oracle loop_hafnian_batch per mode" % cpu_n}}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -438,7 +516,7 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["n40", "loop", "batch", "serve", "precision"], default="n40",
+    ap.add_argument("--workload", choices=["n40", "loop", "batch", "serve", "precision", "sample"], default="n40",
                     help="n40: the benchmark line; the others report the other configurations")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--rates", type=float, nargs="+", default=[100.0, 1000.0, 5000.0, 20000.0])
@@ -446,6 +524,8 @@ def main():
     ap.add_argument("--photons", type=int, nargs=2, default=[8, 44])
     ap.add_argument("--precision-n", type=int, default=20)
     ap.add_argument("--precision-seeds", type=int, default=8)
+    ap.add_argument("--sample-modes", type=int, default=12)
+    ap.add_argument("--samples", type=int, default=256)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -453,7 +533,8 @@ def main():
         return
     if args.workload != "n40":
         if rank == 0:
-            {"loop": run_loop, "batch": run_batch, "serve": run_serve, "precision": run_precision}[args.workload](args)
+            {"loop": run_loop, "batch": run_batch, "serve": run_serve, "precision": run_precision,
+             "sample": run_sample}[args.workload](args)
         return
     run_gpu(args, rank, world, local)
 

@@ -308,6 +308,17 @@ def loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True, precision="double
     return hi
 
 
+def loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True, precision="double", nthreads=None):
+    """Restates thewalrus/loop_hafnian_batch_gamma.py:222-269: for every row k of D the inner
+    loop (:99-117 even, :181-205 odd) is the loop_hafnian_batch sum with displacement D[k]
+    (self-loop weights D[k, 0], D[k, 1]); rows are stacked into an (len(D), N_cutoff + 1) array."""
+    D = np.asarray(D)
+    n = A.shape[0]
+    assert A.shape[1] == n and D.shape[1] == n and len(fixed_reps) == n - 1
+    rows = [loop_hafnian_batch(A, D[k], fixed_reps, N_cutoff, glynn, precision, nthreads) for k in range(len(D))]
+    return np.array(rows, dtype=np.complex128).reshape(len(D), N_cutoff + 1)
+
+
 def powertrace(H, n, precision="double"):
     """charpoly.powertrace(H, n) (restates thewalrus/charpoly.py:301-327)."""
     lib = _load()

@@ -51,6 +51,7 @@ def import_reference(path):
     pkg = types.ModuleType("thewalrus")
     pkg.__path__ = [os.path.join(path, "thewalrus")]
     sys.modules["thewalrus"] = pkg
+    import thewalrus.quantum  # noqa: F401  (resolves the quantum <-> decompositions import cycle)
     import thewalrus.charpoly as cp
     import thewalrus._hafnian as hf
     import thewalrus.loop_hafnian_batch as lb
@@ -153,6 +154,19 @@ def main():
         put("batch", A=B, D=D, fixed=fixed, cutoff=cutoff,
             out=lb.loop_hafnian_batch(B, D, fixed, cutoff))
 
+    # loop_hafnian_batch_gamma (threshold-detector batches): several displacement rows
+    import thewalrus.loop_hafnian_batch_gamma as lbg
+
+    for case in range(6):
+        modes = int(rng.integers(3, 7))
+        calls = wl.batch_loop_calls(count=1, seed=950 + case, modes=modes,
+                                    cutoff=int(rng.integers(1, 5)), max_fixed=2)
+        B, D0, fixed, cutoff = calls[0]
+        nD = int(rng.integers(2, 5))
+        D = np.array([D0 - k * 0.3 * B[:, -1] for k in range(nD)])
+        put("batch_gamma", A=B, D=D, fixed=fixed, cutoff=cutoff,
+            out=lbg.loop_hafnian_batch_gamma(B, D, fixed, cutoff))
+
     # brute-force matchings from thewalrus/reference.py for small n
     for n in (4, 6, 8):
         A = wl.complex_symmetric(n, seed=1000 + n)
@@ -185,6 +199,36 @@ def main():
         if pat.sum() < 2:
             pat[0] += 2
         put("pure", mu=mu, cov=cov, pattern=pat, out=pure_state_amplitude(mu, cov, list(pat)))
+
+    # Gaussian boson sampling (thewalrus/samples.py): a pure and a mixed 5-mode state; samples
+    # for fixed np.random seeds, plus the decomposition the samplers start from
+    import thewalrus.samples as smp
+    from thewalrus.quantum.conversions import Amat
+
+    M = 5
+    U = wl.haar_unitary(M, np.random.default_rng(51))
+    r = np.random.default_rng(52).uniform(0.5, 0.9, size=M)
+    S = sy.interferometer(U) @ sy.squeezing(r)
+    pure = S @ S.T
+    mixed = 0.7 * pure + 0.3 * np.eye(2 * M) * 1.4
+    mean = np.random.default_rng(53).normal(size=2 * M) * 0.3
+    for name, cov in (("pure", pure), ("mixed", mixed)):
+        # the samplers decompose the covariance with the modes re-ordered by mean photon number
+        order = smp.photon_means_order(mean, cov)
+        oo = np.concatenate((order, order + M))
+        cov_r = cov[np.ix_(oo, oo)]
+        T, sqrtW = smp.decompose_cov(cov_r)
+        put("gbs_decomp", cov=cov, mean=mean, order=order, cov_ordered=cov_r, T=T, sqrtW=sqrtW,
+            B=Amat(T)[:M, :M])
+        for seed, (cutoff, maxp, count) in enumerate(((6, 12, 6), (4, 30, 5))):
+            np.random.seed(1000 + seed)
+            samples = smp.hafnian_sample_state(cov, count, mean=mean, cutoff=cutoff, max_photons=maxp)
+            put("gbs_hafnian", cov=cov, mean=mean, seed=1000 + seed, cutoff=cutoff, max_photons=maxp,
+                count=count, out=samples, next_uniform=np.random.random_sample())
+        np.random.seed(77)
+        samples = smp.torontonian_sample_state(cov, 4, mu=mean, fanout=4, cutoff=1, max_photons=30)
+        put("gbs_threshold", cov=cov, mean=mean, seed=77, fanout=4, cutoff=1, max_photons=30, count=4,
+            out=samples, next_uniform=np.random.random_sample())
 
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
     print("wrote %d arrays for %s in %.1fs" % (len(out), counts, time.time() - t0))

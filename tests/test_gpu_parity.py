@@ -55,6 +55,24 @@ def test_batch_vs_reference(golden):
         assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < RTOL
 
 
+def test_batch_gamma_vs_reference(golden):
+    for c in golden["batch_gamma"]:
+        got = tw.loop_hafnian_batch_gamma(c["A"], c["D"], list(c["fixed"]), int(c["cutoff"]))
+        ref = c["out"]
+        assert got.shape == ref.shape
+        assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < RTOL
+
+
+def test_batch_gamma_rows_are_batches():
+    # loop_hafnian_batch_gamma(A, D, f, c)[k] == loop_hafnian_batch(A, D[k], f, c), one plan for all rows
+    B, D0, fixed, cutoff = wl.batch_loop_calls(count=1, seed=12, modes=7, cutoff=3)[0]
+    D = np.array([D0 * (1 + 0.1 * k) - 0.2 * k * B[:, 0] for k in range(5)])
+    got = tw.loop_hafnian_batch_gamma(B, D, list(fixed), cutoff)
+    for k in range(len(D)):
+        one = tw.loop_hafnian_batch(B, D[k], list(fixed), cutoff)
+        assert np.max(np.abs(got[k] - one)) <= 1e-13 * np.max(np.abs(one))
+
+
 def test_brute_force_small():
     for n in (6, 8, 10):
         A = wl.complex_symmetric(n, seed=70 + n)

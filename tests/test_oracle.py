@@ -56,6 +56,17 @@ def test_batch_vs_reference(golden):
         assert np.max(np.abs(got - ref)) / scale < 1e-11
 
 
+def test_batch_gamma_vs_reference(golden):
+    odd_paths = 0
+    for c in golden["batch_gamma"]:
+        got = oracle.loop_hafnian_batch_gamma(c["A"], c["D"], list(c["fixed"]), int(c["cutoff"]))
+        ref = c["out"]
+        assert got.shape == ref.shape
+        assert np.max(np.abs(got - ref)) / np.max(np.abs(ref)) < 1e-11
+        odd_paths += oracle.matched_reps(np.asarray(c["fixed"])[np.nonzero(c["fixed"])])[2] is not None
+    assert 0 < odd_paths < len(golden["batch_gamma"])  # both the even and the odd pairing paths
+
+
 def test_brute_force(golden):
     for c in golden["brute"]:
         A, loop = c["A"], bool(c["loop"])

@@ -1,7 +1,8 @@
 """thewalrus_gb300: the hafnian / loop-hafnian finite-difference sieve of The Walrus on GB300.
 
 Drop-in replacements for ``thewalrus.hafnian``, ``hafnian_repeated``, ``loop_hafnian`` and
-``thewalrus.loop_hafnian_batch.loop_hafnian_batch`` backed by hand-written sm_103a CUDA kernels
+``thewalrus.loop_hafnian_batch.loop_hafnian_batch`` and
+``thewalrus.loop_hafnian_batch_gamma.loop_hafnian_batch_gamma`` backed by hand-written sm_103a CUDA kernels
 (``csrc/``) behind a C ABI (``include/walrus_gb300.h``).
 """
 from ._hafnian import (
@@ -9,6 +10,7 @@ from ._hafnian import (
     hafnian_repeated,
     loop_hafnian,
     loop_hafnian_batch,
+    loop_hafnian_batch_gamma,
     hafnian_batch,
     input_validation,
     reduction,
@@ -16,6 +18,7 @@ from ._hafnian import (
     prepare_hafnian,
     prepare_loop_hafnian,
     prepare_loop_hafnian_batch,
+    prepare_loop_hafnian_batch_gamma,
 )
 from . import _native as native
 
@@ -26,6 +29,7 @@ __all__ = [
     "hafnian_repeated",
     "loop_hafnian",
     "loop_hafnian_batch",
+    "loop_hafnian_batch_gamma",
     "hafnian_batch",
     "input_validation",
     "reduction",
@@ -33,6 +37,7 @@ __all__ = [
     "prepare_hafnian",
     "prepare_loop_hafnian",
     "prepare_loop_hafnian_batch",
+    "prepare_loop_hafnian_batch_gamma",
     "native",
     "version",
 ]

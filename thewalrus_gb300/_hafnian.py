@@ -281,6 +281,32 @@ def loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True, precision=None):
     return nat.run([prep], precision or DEFAULT_PRECISION)
 
 
+def prepare_loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True):
+    """Host preparation of ``loop_hafnian_batch_gamma`` (loop_hafnian_batch_gamma.py:222-269).
+
+    D holds one displacement vector per row.  The reference's inner loop over rows k
+    (loop_hafnian_batch_gamma.py:99-117 and :181-205) evaluates, for each k, exactly the
+    ``loop_hafnian_batch`` sum with D[k] (self-loop weights D[k, 0] and D[k, 1], the same
+    AX_S and oddV), so each row becomes one batch instance; all rows run in one plan.
+    """
+    D = np.asarray(D)
+    n = A.shape[0]
+    assert A.shape[1] == n
+    assert D.ndim == 2 and D.shape[1] == n
+    assert len(fixed_reps) == n - 1
+    return [prepare_loop_hafnian_batch(A, D[k], fixed_reps, N_cutoff, glynn) for k in range(D.shape[0])]
+
+
+def loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True, precision=None):
+    """Loop hafnians for every photon number 0..N_cutoff of the last mode, for each row of D
+    (threshold-detector sampling); returns an array of shape (len(D), N_cutoff + 1)."""
+    preps = prepare_loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn)
+    if not preps:
+        return np.zeros((0, N_cutoff + 1), dtype=np.complex128)
+    vals = nat.run(preps, precision or DEFAULT_PRECISION)
+    return vals.reshape(len(preps), -1)
+
+
 def hafnian_batch(matrices, loop=False, rtol=1e-05, atol=1e-08, method="glynn", precision=None,
                   validate=True):
     """Hafnians of many matrices of uneven size in one persistent launch per arithmetic class.

@@ -15,8 +15,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwalrus_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["sieve.cu", "noalloc.cu"]
-DEPS = ["sieve.cu", "noalloc.cu", "sieve_kernel.cuh", "arith.cuh", "host_common.h"]
+SOURCES = ["sieve.cu", "noalloc.cu", "kernels_c64.cu", "kernels_cdf.cu", "kernels_f64.cu", "kernels_fdf.cu"]
+DEPS = SOURCES + ["sieve_kernel.cuh", "arith.cuh", "host_common.h", "kernels.h", "kernels_unit.cuh"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-shared"]
 

@@ -32,6 +32,19 @@ __device__ __forceinline__ unsigned long long absbits_d(double x) {
 }
 __device__ __forceinline__ unsigned int absbits_f(float x) { return (unsigned)__float_as_int(x) & 0x7fffffffu; }
 
+// Deflation threshold of a pivot column: the key (magnitude bits) of k * 2^-44 for FP64 keys and
+// k * 2^-40 for the FP32 high parts of double-float keys (0 when that leaves the normal range).
+// Subdiagonal candidates at or below it are rounding residues of an exact cancellation (terms
+// whose matrix repeats a row, such as the two ends of the batch edge) and are treated as zero.
+__device__ __forceinline__ unsigned long long key_shift_d(unsigned long long k) {
+  constexpr unsigned long long sh = 44ull << 52;
+  return k > sh ? k - sh : 0ull;
+}
+__device__ __forceinline__ unsigned long long key_shift_f(unsigned long long k) {
+  constexpr unsigned long long sh = 40ull << 23;
+  return k > sh ? k - sh : 0ull;
+}
+
 // 1/x for the pivots: the PTX approximate reciprocal (rcp.approx.ftz.f64) refined by two Newton
 // steps r <- r + r(1 - x r), which square the relative error each time; inputs whose exponent
 // leaves the approximation's safe range take the IEEE division instead.
@@ -128,6 +141,7 @@ struct Ar<double> {
   __device__ static __forceinline__ S from_c64(c64 v) { return v.re; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {a, 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a); }
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_d(k); }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a) == 0; }
   __device__ static __forceinline__ S recip(S a) { return recip_newton(a); }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
@@ -165,9 +179,10 @@ struct Ar<c64> {
   __device__ static __forceinline__ S from_c64(c64 v) { return v; }
   __device__ static __forceinline__ c64 to_c64(S a) { return a; }
   __device__ static __forceinline__ unsigned long long key(S a) {
-    unsigned long long x = absbits_d(a.re), y = absbits_d(a.im);
+    const unsigned long long x = absbits_d(a.re), y = absbits_d(a.im);
     return x > y ? x : y;
   }
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_d(k); }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re) | absbits_d(a.im)) == 0; }
   __device__ static __forceinline__ S recip(S a) {
     const double d = recip_newton(::fma(a.re, a.re, a.im * a.im));
@@ -204,6 +219,7 @@ struct Ar<dfr> {
   __device__ static __forceinline__ S from_c64(c64 v) { return df_from_d(v.re); }
   __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a), 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_f(a.hi); }
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_f(k); }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_f(a.hi) == 0; }
   __device__ static __forceinline__ S recip(S a) { return df_from_d(1.0 / df_to_d(a)); }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
@@ -247,9 +263,10 @@ struct Ar<cdf> {
   __device__ static __forceinline__ S from_c64(c64 v) { return {df_from_d(v.re), df_from_d(v.im)}; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a.re), df_to_d(a.im)}; }
   __device__ static __forceinline__ unsigned long long key(S a) {
-    unsigned x = absbits_f(a.re.hi), y = absbits_f(a.im.hi);
+    const unsigned x = absbits_f(a.re.hi), y = absbits_f(a.im.hi);
     return x > y ? x : y;
   }
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_f(k); }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_f(a.re.hi) | absbits_f(a.im.hi)) == 0; }
   __device__ static __forceinline__ S recip(S a) {
     c64 z = to_c64(a);

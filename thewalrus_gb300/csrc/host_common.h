@@ -5,14 +5,23 @@
 #include <algorithm>
 #include <vector>
 
+#include "kernels.h"
 #include "sieve_kernel.cuh"
 
 namespace wg {
+
+// kernel launch and occupancy by scalar class (the kernels live in kernels_*.cu)
+static inline cudaError_t sieve_launch(int stype, int ns, const SieveParams& p, int ctas, int wpc, cudaStream_t st);
+static inline int sieve_occupancy(int stype, int ns, int wpc, int smem);
+static inline cudaError_t sieve_tables_all(const double* binom, const double* inv);
 
 // scalar classes
 enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3 };
 static size_t stype_bytes(int st) { return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16; }
 
+// register classes: rows of the term tile per row lane (8 row lanes).  Row slots beyond the
+// tile are skipped by a warp-uniform branch, so a class larger than needed costs registers, not
+// FP64 issue slots; a few classes keep the build small.
 static const int NS_CPLX[] = {4, 6, 8, 10};
 static const int NS_REAL[] = {4, 8, 12};
 
@@ -25,6 +34,32 @@ static inline int pick_ns(int stype, int rows) {
       if (8 * ns >= rows) return ns;
   }
   return -1;
+}
+
+static inline cudaError_t sieve_launch(int stype, int ns, const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
+  switch (stype) {
+    case ST_CPLX64: return sieve_launch_c64(ns, p, ctas, wpc, st);
+    case ST_CPLXDF: return sieve_launch_cdf(ns, p, ctas, wpc, st);
+    case ST_REAL64: return sieve_launch_f64(ns, p, ctas, wpc, st);
+    default: return sieve_launch_fdf(ns, p, ctas, wpc, st);
+  }
+}
+
+static inline int sieve_occupancy(int stype, int ns, int wpc, int smem) {
+  switch (stype) {
+    case ST_CPLX64: return sieve_occupancy_c64(ns, wpc, smem);
+    case ST_CPLXDF: return sieve_occupancy_cdf(ns, wpc, smem);
+    case ST_REAL64: return sieve_occupancy_f64(ns, wpc, smem);
+    default: return sieve_occupancy_fdf(ns, wpc, smem);
+  }
+}
+
+static inline cudaError_t sieve_tables_all(const double* binom, const double* inv) {
+  cudaError_t e = sieve_tables_c64(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_cdf(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_f64(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_fdf(binom, inv);
+  return e;
 }
 
 // tilewin: La Budde's coefficient rows live in dead tile columns (only rows 0..2 need `win`)

@@ -106,8 +106,7 @@ static int setup(int dev, DeviceState** out) {
     static LbOwner2 own2[(LB2_KMAX + 1) * (LB2_KMAX + 1)];
     for (int k = 0; k <= LB2_KMAX; ++k)
       if (!lb_schedule2(k, &lanes2[k * 32], &own2[k * (LB2_KMAX + 1)])) return err(WG_EINVAL, "no La Budde schedule");
-    if (cudaMemcpyToSymbol(c_binom, binom, sizeof(binom)) != cudaSuccess ||
-        cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)) != cudaSuccess ||
+    if (sieve_tables_all(&binom[0][0], inv) != cudaSuccess ||
         cudaMemcpyToSymbol(g_lane_tab, lanes, sizeof(lanes)) != cudaSuccess ||
         cudaMemcpyToSymbol(g_own_tab, own, sizeof(own)) != cudaSuccess ||
         cudaMemcpyToSymbol(g_lane2_tab, lanes2, sizeof(lanes2)) != cudaSuccess ||
@@ -138,25 +137,6 @@ static __global__ void noalloc_setup_kernel(unsigned char* scratch, const InstDe
     ch.t1 = inst.steps * (c + 1) / nchunks;
     reinterpret_cast<ChunkDev*>(scratch + kOffChunks)[c] = ch;
   }
-}
-
-template <class S, int NS>
-static cudaError_t launch(const SieveParams& p, int wpc, int ctas, cudaStream_t st) {
-  auto k = sieve_kernel<S, NS>;
-  const int smem = wpc * p.L.bytes;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  k<<<ctas, 32 * wpc, smem, st>>>(p);
-  return cudaGetLastError();
-}
-
-template <class S, int NS>
-static int resident_ctas(int wpc, int smem) {
-  int nb = 0;
-  auto k = sieve_kernel<S, NS>;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpc, smem) != cudaSuccess) return 0;
-  return nb;
 }
 
 }  // namespace noalloc
@@ -218,21 +198,7 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
                                    all_odd && d.K < m_max);
   const int wpc = std::min(8, (227 * 1024) / L.bytes);
   if (wpc < 1) return err(WG_EINVAL, "size beyond the maximum: per-warp workspace does not fit");
-  int per_sm = 0;
-  if (st == ST_CPLX64) {
-    switch (ns) {
-      case 4: per_sm = resident_ctas<c64, 4>(wpc, wpc * L.bytes); break;
-      case 6: per_sm = resident_ctas<c64, 6>(wpc, wpc * L.bytes); break;
-      case 8: per_sm = resident_ctas<c64, 8>(wpc, wpc * L.bytes); break;
-      default: per_sm = resident_ctas<c64, 10>(wpc, wpc * L.bytes); break;
-    }
-  } else {
-    switch (ns) {
-      case 4: per_sm = resident_ctas<double, 4>(wpc, wpc * L.bytes); break;
-      case 8: per_sm = resident_ctas<double, 8>(wpc, wpc * L.bytes); break;
-      default: per_sm = resident_ctas<double, 12>(wpc, wpc * L.bytes); break;
-    }
-  }
+  const int per_sm = sieve_occupancy(st, ns, wpc, wpc * L.bytes);
   if (per_sm < 1) return err(WG_ECUDA, "sieve kernel cannot be resident");
   const long long resident = (long long)ds->sms * per_sm * wpc;
   long long nch = std::min<long long>(steps, 4 * resident);
@@ -266,21 +232,7 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   p.err = nullptr;
   p.L = L;
   const int ctas = (int)std::max<long long>(1, std::min<long long>((long long)ds->sms * per_sm, (nch + wpc - 1) / wpc));
-  cudaError_t e;
-  if (st == ST_CPLX64) {
-    switch (ns) {
-      case 4: e = launch<c64, 4>(p, wpc, ctas, s); break;
-      case 6: e = launch<c64, 6>(p, wpc, ctas, s); break;
-      case 8: e = launch<c64, 8>(p, wpc, ctas, s); break;
-      default: e = launch<c64, 10>(p, wpc, ctas, s); break;
-    }
-  } else {
-    switch (ns) {
-      case 4: e = launch<double, 4>(p, wpc, ctas, s); break;
-      case 8: e = launch<double, 8>(p, wpc, ctas, s); break;
-      default: e = launch<double, 12>(p, wpc, ctas, s); break;
-    }
-  }
+  const cudaError_t e = sieve_launch(st, ns, p, ctas, wpc, s);
   if (e != cudaSuccess) return err(WG_ECUDA, "sieve kernel launch failed");
   reduce_kernel<<<1, 32, 0, s>>>(p.inst, 1, p.partials, reinterpret_cast<const double*>(scr + kOffScale),
                                  reinterpret_cast<double2*>(out_dev), p.counter, 1, 1);

@@ -79,8 +79,7 @@ static int ensure_init(int device) {
   double inv[256];
   inv[0] = 0;
   for (int k = 1; k < 256; ++k) inv[k] = 1.0 / (double)k;
-  CK(cudaMemcpyToSymbol(c_binom, binom, sizeof(binom)));
-  CK(cudaMemcpyToSymbol(c_inv, inv, sizeof(inv)));
+  CK(sieve_tables_all(&binom[0][0], inv));
   // La Budde lane schedules for every triangle size (built once, kept for the process lifetime)
   std::vector<LbLane> lanes((LB_KMAX + 1) * 32);
   std::vector<LbOwner> own((LB_KMAX + 1) * (LB_KMAX + 1));
@@ -163,59 +162,6 @@ struct wg_state {
 
 namespace wg {
 
-
-template <class S, int NS>
-static cudaError_t launch_one(const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
-  auto k = sieve_kernel<S, NS>;
-  const int smem = wpc * p.L.bytes;
-  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  k<<<ctas, 32 * wpc, smem, st>>>(p);
-  return cudaGetLastError();
-}
-
-template <class S, int NS>
-static int occupancy_one(int wpc, int smem) {
-  int nb = 0;
-  auto k = sieve_kernel<S, NS>;
-  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpc, smem) != cudaSuccess) return 0;
-  return nb;
-}
-
-#define WG_DISPATCH(ST, NS, CALL)                              \
-  switch (ST) {                                                \
-    case ST_CPLX64:                                            \
-      switch (NS) {                                            \
-        case 4: CALL(c64, 4); break;                           \
-        case 6: CALL(c64, 6); break;                           \
-        case 8: CALL(c64, 8); break;                           \
-        default: CALL(c64, 10); break;                         \
-      }                                                        \
-      break;                                                   \
-    case ST_CPLXDF:                                            \
-      switch (NS) {                                            \
-        case 4: CALL(cdf, 4); break;                           \
-        case 6: CALL(cdf, 6); break;                           \
-        case 8: CALL(cdf, 8); break;                           \
-        default: CALL(cdf, 10); break;                         \
-      }                                                        \
-      break;                                                   \
-    case ST_REAL64:                                            \
-      switch (NS) {                                            \
-        case 4: CALL(double, 4); break;                        \
-        case 8: CALL(double, 8); break;                        \
-        default: CALL(double, 12); break;                      \
-      }                                                        \
-      break;                                                   \
-    default:                                                   \
-      switch (NS) {                                            \
-        case 4: CALL(dfr, 4); break;                           \
-        case 8: CALL(dfr, 8); break;                           \
-        default: CALL(dfr, 12); break;                         \
-      }                                                        \
-      break;                                                   \
-  }
 
 
 static inline void put_scalar(unsigned char* dst, int st, double re, double im) {
@@ -614,9 +560,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     int wpc = std::min(wpc_cap, max_smem / G.L.bytes);
     if (wpc < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
     int per_sm = 0;
-#define WG_OCC(S, NS) per_sm = occupancy_one<S, NS>(wpc, wpc * G.L.bytes)
-    WG_DISPATCH(G.stype, G.ns, WG_OCC)
-#undef WG_OCC
+    per_sm = sieve_occupancy(G.stype, G.ns, wpc, wpc * G.L.bytes);
     if (per_sm < 1) {
       cudaGetLastError();
       return fail(WG_ECUDA, "sieve kernel cannot be resident (workspace %d B x %d warps)", G.L.bytes, wpc);
@@ -742,10 +686,7 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
     p.counter = pl->d_counters + g;
     p.err = pl->d_err;
     p.L = G.L;
-    cudaError_t e = cudaSuccess;
-#define WG_LAUNCH(S, NS) e = launch_one<S, NS>(p, G.ctas, G.wpc, st)
-    WG_DISPATCH(G.stype, G.ns, WG_LAUNCH)
-#undef WG_LAUNCH
+    const cudaError_t e = sieve_launch(G.stype, G.ns, p, G.ctas, G.wpc, st);
     if (e != cudaSuccess) return fail(WG_ECUDA, "sieve launch: %s", cudaGetErrorString(e));
   }
   const int ninst = (int)pl->inst.size();

@@ -174,21 +174,28 @@ __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
 // double-float scalars use the classic form: multipliers l = W[a][j]/piv (|l| <= 1),
 // W[j+1][j] keeps the pivot and column j+1 += sum_b W[:,b] l_b.
 template <class S, int NS>
-__device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, int rows, int ldw) {
+__device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, int rows, int ldw, int nb) {
   using A = Ar<S>;
   using Comp = typename A::Comp;
   const int lane = threadIdx.x & 31;
   const int r8 = lane & 7, c4 = lane >> 3;
   constexpr int NCOMP = NS * A::NC;
-  static_assert(NCOMP % 4 == 0, "slot components must split over 4 column lanes");
+  constexpr int NCP = (NCOMP + 3) / 4 * 4;  // padded so the slots split over the 4 column lanes
 
   for (int j = 0; j + 1 < mb; ++j) {
-    // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1 (ties: lowest row)
-    unsigned long long bk = 0;
+    // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1 (ties: lowest row).  The
+    // same pass takes each lane's largest key over the column's block rows nb..j (uk, never
+    // reduced): the column is deflated when some lane's uk puts the best candidate at or below
+    // the deflation threshold, i.e. when max uk does -- one vote, off the shuffle chain.
+    unsigned long long bk = 0, uk = 0;
     int bi = j + 1;
-    for (int a = j + 1 + lane; a < mb; a += 32) {
-      unsigned long long k = A::key(W[a * ldw + j]);
-      if (k > bk) { bk = k; bi = a; }
+    for (int a = nb + lane; a < mb; a += 32) {
+      const unsigned long long k = A::key(W[a * ldw + j]);
+      if (a > j) {
+        if (k > bk) { bk = k; bi = a; }
+      } else {
+        uk = k > uk ? k : uk;
+      }
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
@@ -196,8 +203,10 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
       int oi = __shfl_xor_sync(0xffffffffu, bi, off);
       if (ok > bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
     }
-    if (bk == 0) {  // nothing to eliminate: subdiagonal entry is an exact zero
-      if (lane == 0) W[(j + 1) * ldw + j] = A::zero();
+    if (__any_sync(0xffffffffu, bk <= A::key_deflate(uk))) {
+      // nothing to eliminate: the candidates are zero or rounding residues of an exact
+      // cancellation; the subdiagonal becomes an exact zero and the column below it is cleared
+      for (int a = j + 1 + lane; a < mb; a += 32) W[a * ldw + j] = A::zero();
       __syncwarp();
       continue;
     }
@@ -267,34 +276,36 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
       }
     }
     // reduce-scatter across the 4 column lanes (lane bits 3 and 4)
-    Comp v[NCOMP];
+    Comp v[NCP];
 #pragma unroll
     for (int s = 0; s < NS; ++s)
 #pragma unroll
       for (int c = 0; c < A::NC; ++c) v[s * A::NC + c] = A::comp(acc[s], c);
-    const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
-    Comp u[NCOMP / 2];
 #pragma unroll
-    for (int i = 0; i < NCOMP / 2; ++i) {
-      Comp send = h1 ? v[i] : v[NCOMP / 2 + i];
-      Comp keep = h1 ? v[NCOMP / 2 + i] : v[i];
+    for (int i = NCOMP; i < NCP; ++i) v[i] = A::comp(A::zero(), 0);
+    const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
+    Comp u[NCP / 2];
+#pragma unroll
+    for (int i = 0; i < NCP / 2; ++i) {
+      Comp send = h1 ? v[i] : v[NCP / 2 + i];
+      Comp keep = h1 ? v[NCP / 2 + i] : v[i];
       u[i] = A::cadd(keep, A::shfl_xor(send, 16));
     }
-    Comp z[NCOMP / 4];
+    Comp z[NCP / 4];
 #pragma unroll
-    for (int i = 0; i < NCOMP / 4; ++i) {
-      Comp send = h2 ? u[i] : u[NCOMP / 4 + i];
-      Comp keep = h2 ? u[NCOMP / 4 + i] : u[i];
+    for (int i = 0; i < NCP / 4; ++i) {
+      Comp send = h2 ? u[i] : u[NCP / 4 + i];
+      Comp keep = h2 ? u[NCP / 4 + i] : u[i];
       z[i] = A::cadd(keep, A::shfl_xor(send, 8));
     }
     __syncwarp();
-    const int base = (h1 ? NCOMP / 2 : 0) + (h2 ? NCOMP / 4 : 0);
+    const int base = (h1 ? NCP / 2 : 0) + (h2 ? NCP / 4 : 0);
 #pragma unroll
-    for (int i = 0; i < NCOMP / 4; ++i) {
+    for (int i = 0; i < NCP / 4; ++i) {
       const int vi = base + i;
       const int s = vi / A::NC, part = vi % A::NC;
       const int a = r8 + 8 * s;
-      if (a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
+      if (vi < NCOMP && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
     }
     __syncwarp();
   }
@@ -675,7 +686,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
         }
       }
       __syncwarp();
-      hessenberg_elim<S, NS>(W, xv, mb, rows, ldw);
+      hessenberg_elim<S, NS>(W, xv, mb, rows, ldw, nb);
       // loop variants: Krylov data of the border first (La Budde then reuses the tile)
       if (kind != KIND_PLAIN) loop_krylov<S>(W, ldw, m, mb, ne, I.K, xv, eser, lam, mu, mu0);
       // characteristic polynomial coefficients of the block (xv caches the subdiagonal)

@@ -12,6 +12,8 @@ hafnian / loop-hafnian path:
 * ``gaussian_state_loop(modes, seed, ...)``: reduced loop-hafnian input of a synthetic Gaussian
   state: Haar unitary U, squeezing r_i ~ U(0.3, 0.8), B = U diag(tanh r) U^T, A = B (+) B*,
   diagonal gamma ~ CN(0, 0.1) and a photon pattern with at most ``max_rep`` photons per mode.
+* ``gaussian_state_cov(modes, seed, ...)``: covariance and means of a lossy squeezed, displaced
+  state behind a Haar interferometer (the samplers' input).
 
 Haar sampling follows the QR-with-phase-correction recipe that
 ``thewalrus/random.py:115-134`` (``random_interferometer``) uses.
@@ -25,6 +27,7 @@ __all__ = [
     "adjacency01",
     "haar_unitary",
     "gaussian_state_loop",
+    "gaussian_state_cov",
     "photon_pattern",
     "batch_instances",
     "batch_loop_calls",
@@ -101,6 +104,21 @@ def gaussian_state_loop(modes=20, seed=1, photons=40, max_rep=3):
     nvec = photon_pattern(modes, photons // 2, max_rep, rng)
     rpt = np.concatenate([nvec, nvec])
     return A, gamma, rpt
+
+
+def gaussian_state_cov(modes=12, seed=21, r_range=(0.5, 0.9), transmission=0.8, disp=0.3):
+    """xp-covariance (hbar = 2) and means of a synthetic lossy GBS state: single-mode squeezers
+    r_i ~ U(r_range) (diag(e^-r, e^r)), a Haar interferometer ([[Re U, -Im U], [Im U, Re U]]),
+    uniform transmission (cov -> t cov + (1 - t) I) and means ~ N(0, disp^2)."""
+    rng = np.random.default_rng(seed)
+    U = haar_unitary(modes, rng)
+    r = rng.uniform(*r_range, size=modes)
+    Sq = np.diag(np.concatenate([np.exp(-r), np.exp(r)]))
+    O = np.block([[U.real, -U.imag], [U.imag, U.real]])
+    S = O @ Sq
+    cov = transmission * (S @ S.T) + (1 - transmission) * np.identity(2 * modes)
+    mean = rng.normal(size=2 * modes) * disp
+    return cov, mean
 
 
 def batch_instances(count=4096, seed=2, n_min=8, n_max=40):
