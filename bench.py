@@ -33,6 +33,9 @@ sys.path.insert(0, ROOT)
 N_MATRIX = 40
 METRIC = "n=40 hafnians/s (complex128, Glynn sieve)"
 UNIT = "hafnians/s"
+# The published wall time of one 40x40 complex hafnian (thewalrus hafnian tutorial, 4 threads of
+# an AMD A12-9800, the library's earlier C++ implementation): vs_baseline = value x 41.32 s.
+PUBLISHED_N40_SECONDS = 41.32
 
 
 def workload(n=N_MATRIX):
@@ -146,8 +149,10 @@ def run_reference(args, rank, world):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
-        "data": "synthetic", "config": {"workload": "hafnian 40x40 complex128, seed 0"},
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": value * PUBLISHED_N40_SECONDS, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": "hafnian 40x40 complex128 (G+G^T)/2, seed 0, 524288 sieve terms",
+                   "precision": "fp64", "parallelism": "%d host threads" % threads},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -225,19 +230,20 @@ def run_gpu(args, rank, world, local):
     mean_s = total_ms / args.steps * 1e-3
     achieved = flops / mean_s / 1e12
     peak = fp64_peak if args.precision == "fp64" else fp32_peak
+    # DRAM bytes per sieve launch from the committed ncu capture of this workload (FP64, n = 40)
     traffic = None
-    prof = os.path.join(ROOT, "profiles", "sieve_c64_n40_traffic.json")
-    if os.path.exists(prof):
-        try:
-            traffic = json.load(open(prof)).get("bytes_per_launch")
-        except (OSError, ValueError):
-            traffic = None
+    prof = os.path.join(ROOT, "profiles", "sieve_c64_n40_traffic.md")
+    if n == N_MATRIX and args.precision == "fp64" and os.path.exists(prof):
+        for ln in open(prof):
+            if ln.startswith("bytes_per_launch:"):
+                traffic = float(ln.split(":", 1)[1])
     if rank != 0:
         return
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "df32",
+        "scaling": "weak", "vs_baseline": (value * PUBLISHED_N40_SECONDS if n == N_MATRIX else None),
+        "dtype": "f64" if args.precision == "fp64" else "df32",
         "data": "synthetic",
         "config": {"workload": "hafnian %dx%d complex128 (G+G^T)/2, seed 0, %d sieve terms"
                                % (n, n, 2 ** (n // 2 - 1)),
