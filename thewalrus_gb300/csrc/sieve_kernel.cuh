@@ -477,37 +477,44 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
   __syncwarp();
 }
 
-// g = (sum_j c_j eta^j)^(-1/2) up to degree G:  n g_n = -sum_{i=1}^{n} c_i (n - i/2) g_{n-i}
+// g = (sum_j c_j eta^j)^(-1/2) up to degree G:  n g_n = -sum_{i=1}^{n} c_i (n - i/2) g_{n-i}.
+// Right-looking: once g_k is final, every later coefficient n (n - k <= Kc) takes its term
+// c_{n-k} ((n + k)/2) g_k at once, one lane per coefficient; g_{k+1} is then complete and is
+// finalised by its lane.  No warp reductions: 2 DMUL + 4 DFMA per step and lane.
 template <class S>
 __device__ void inv_sqrt_series(const S* __restrict__ cpoly, int Kc, S* __restrict__ g, int G) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
-  if (lane == 0) g[0] = A::one();
+  for (int n = lane; n <= G; n += 32) g[n] = n == 0 ? A::one() : A::zero();
   __syncwarp();
-  for (int nn = 1; nn <= G; ++nn) {
-    const int lim = nn < Kc ? nn : Kc;
-    S part = A::zero();
-    for (int i = lane + 1; i <= lim; i += 32)
-      part = A::fma(A::scale(cpoly[i], (double)nn - 0.5 * (double)i), g[nn - i], part);
-    part = warp_sum(part);
-    if (lane == 0) g[nn] = A::scale(part, -inv_int(nn));
+  for (int k = 0; k < G; ++k) {
+    const S gk = g[k];
+    const int hi = (k + Kc) < G ? (k + Kc) : G;
+    for (int n = k + 1 + lane; n <= hi; n += 32) {
+      S acc = A::fma(cpoly[n - k], A::scale(gk, 0.5 * (double)(n + k)), g[n]);
+      if (n == k + 1) acc = A::scale(acc, -inv_int(n));
+      g[n] = acc;
+    }
     __syncwarp();
   }
 }
 
-// e = exp(sum_{l=1}^{Q} q_l z^l) up to degree G:  n e_n = sum_{l=1}^{n} l q_l e_{n-l}
+// e = exp(sum_{l=1}^{Q} q_l z^l) up to degree G:  n e_n = sum_{l=1}^{n} l q_l e_{n-l}, in the same
+// right-looking form (q is read as l q_l on the fly).
 template <class S>
 __device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, int G) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
-  if (lane == 0) e[0] = A::one();
+  for (int n = lane; n <= G; n += 32) e[n] = n == 0 ? A::one() : A::zero();
   __syncwarp();
-  for (int nn = 1; nn <= G; ++nn) {
-    const int lim = nn < Q ? nn : Q;
-    S part = A::zero();
-    for (int l = lane + 1; l <= lim; l += 32) part = A::fma(A::scale(q[l], (double)l), e[nn - l], part);
-    part = warp_sum(part);
-    if (lane == 0) e[nn] = A::scale(part, inv_int(nn));
+  for (int k = 0; k < G; ++k) {
+    const S ek = e[k];
+    const int hi = (k + Q) < G ? (k + Q) : G;
+    for (int n = k + 1 + lane; n <= hi; n += 32) {
+      S acc = A::fma(A::scale(q[n - k], (double)(n - k)), ek, e[n]);
+      if (n == k + 1) acc = A::scale(acc, inv_int(n));
+      e[n] = acc;
+    }
     __syncwarp();
   }
 }
