@@ -240,10 +240,14 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
     // --- phase A: rows j+2..mb-1, cols j+1..mb-1: W[a][b] -= x[a] * W[j+1][b]  (flattened)
     const int w = mb - j - 1;
     if (mb - j - 2 > 0) {
+      // elements e = lane + 32 k (row-major over rows j+2.., cols j+1..) stepped without divisions;
+      // full passes of 128 need no predicates, and the tail runs only the slots that hold elements
+      // (a predicated FP64 instruction costs its issue slot even when no lane executes it)
+      const int total = (mb - j - 2) * w;
       const int dr = 32 / w, dc = 32 % w;
       int a = j + 2 + lane / w, b = j + 1 + lane % w;
       const S* prow = W + (j + 1) * ldw;
-      while (a < mb) {  // four independent elements per pass: loads issued before the stores
+      for (int pass = total >> 7; pass > 0; --pass) {  // four independent elements, loads before stores
         int aa[4], bb[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
@@ -255,11 +259,15 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
         }
         S vv[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (aa[u] < mb) vv[u] = A::fnma(xv[aa[u]], prow[bb[u]], W[aa[u] * ldw + bb[u]]);
+        for (int u = 0; u < 4; ++u) vv[u] = A::fnma(xv[aa[u]], prow[bb[u]], W[aa[u] * ldw + bb[u]]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u)
-          if (aa[u] < mb) W[aa[u] * ldw + bb[u]] = vv[u];
+        for (int u = 0; u < 4; ++u) W[aa[u] * ldw + bb[u]] = vv[u];
+      }
+      for (int rem = total & 127; rem > 0; rem -= 32) {
+        if (a < mb) W[a * ldw + b] = A::fnma(xv[a], prow[b], W[a * ldw + b]);
+        b += dc;
+        a += dr;
+        if (b >= mb) { b -= w; a += 1; }
       }
     }
     __syncwarp();
@@ -522,6 +530,9 @@ __device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, in
 // Warp-cooperative Krylov data of the loop variants, on the reduced tile.
 // v_1 = e_1, v_{t+1} = H v_t (H the m x m block).  For t = 1..T:
 //   lam[t] = d * x.v_t  (x = tile row 0, cols 1..m),  mu[t] = d * y.v_t (tile row mb), mu0 likewise.
+// Column form, one lane per row: the "rows" of one step are x (virtual row 0), the Hessenberg
+// rows 1..min(t+1, m) and the extra rows y, y0, so the dot products are rows of the same sweep
+// over s (no warp reductions); v ping-pongs between two buffers.
 template <class S>
 __device__ void loop_krylov(const S* __restrict__ W, int ldw, int m, int mb, int ne, int T, S* __restrict__ v,
                             S* __restrict__ vn, S* __restrict__ lam, S* __restrict__ mu, S* __restrict__ mu0) {
@@ -540,33 +551,49 @@ __device__ void loop_krylov(const S* __restrict__ W, int ldw, int m, int mb, int
   const S d = W[1 * ldw + 0];
   for (int s = lane; s <= m; s += 32) v[s] = (s == 1) ? A::one() : A::zero();
   __syncwarp();
+  constexpr int SLOTS = 3;  // virtual rows lane, lane + 32, lane + 64 (m + 1 + ne <= 96)
   for (int t = 1; t <= T; ++t) {
-    const int sup = t < m ? t : m;  // support of v_t: block indices 1..sup
-    S pl = A::zero(), pm = A::zero(), p0 = A::zero();
-    for (int s = lane + 1; s <= sup; s += 32) {
-      pl = A::fma(W[0 * ldw + s], v[s], pl);
-      if (ne > 0) pm = A::fma(W[mb * ldw + s], v[s], pm);
-      if (ne > 1) p0 = A::fma(W[(mb + 1) * ldw + s], v[s], p0);
+    const int sup = t < m ? t : m;                            // support of v_t: 1..sup
+    const int nsup = t == T ? 0 : ((t + 1) < m ? (t + 1) : m);  // rows of v_{t+1} (none at the end)
+    const int nv = nsup + 1 + ne;                             // virtual rows: x, H rows, extra rows
+    int row[SLOTS], lo[SLOTS];
+    S acc[SLOTS];
+#pragma unroll
+    for (int k = 0; k < SLOTS; ++k) {
+      const int vr = lane + 32 * k;
+      acc[k] = A::zero();
+      if (vr == 0) { row[k] = 0; lo[k] = 1; }                        // x
+      else if (vr <= nsup) { row[k] = vr; lo[k] = vr > 1 ? vr - 1 : 1; }  // Hessenberg row
+      else if (vr < nv) { row[k] = mb + (vr - nsup - 1); lo[k] = 1; }  // y, y0
+      else { row[k] = -1; lo[k] = sup + 1; }
     }
-    pl = warp_sum(pl);
-    if (ne > 0) pm = warp_sum(pm);
-    if (ne > 1) p0 = warp_sum(p0);
-    if (lane == 0) {
-      lam[t] = A::mul(d, pl);
-      if (ne > 0) mu[t] = A::mul(d, pm);
-      if (ne > 1) mu0[t] = A::mul(d, p0);
+    if (nv <= 32) {  // one virtual row per lane (t + ne < 31): a loop that issues one FMA per s
+      const S* wr = W + (row[0] >= 0 ? row[0] : 0) * ldw;
+      const int l0 = row[0] >= 0 ? lo[0] : sup + 1;
+      for (int s = 1; s <= sup; ++s) {
+        const S vs = v[s];
+        if (s >= l0) acc[0] = A::fma(wr[s], vs, acc[0]);
+      }
+    } else {
+      for (int s = 1; s <= sup; ++s) {
+        const S vs = v[s];
+#pragma unroll
+        for (int k = 0; k < SLOTS; ++k)
+          if (32 * k < nv && s >= lo[k] && row[k] >= 0) acc[k] = A::fma(W[row[k] * ldw + s], vs, acc[k]);
+      }
     }
-    if (t == T) break;
-    const int nsup = (t + 1) < m ? (t + 1) : m;
-    for (int rho = lane + 1; rho <= nsup; rho += 32) {
-      S acc = A::zero();
-      const int s0 = rho > 1 ? rho - 1 : 1;
-      for (int s = s0; s <= sup; ++s) acc = A::fma(W[rho * ldw + s], v[s], acc);
-      vn[rho] = acc;
+#pragma unroll
+    for (int k = 0; k < SLOTS; ++k) {
+      const int vr = lane + 32 * k;
+      if (vr == 0) lam[t] = A::mul(d, acc[k]);
+      else if (vr <= nsup) vn[vr] = acc[k];
+      else if (vr == nsup + 1 && ne > 0) mu[t] = A::mul(d, acc[k]);
+      else if (vr == nsup + 2 && ne > 1) mu0[t] = A::mul(d, acc[k]);
     }
     __syncwarp();
-    for (int rho = lane + 1; rho <= nsup; rho += 32) v[rho] = vn[rho];
-    __syncwarp();
+    S* sw = v;
+    v = vn;
+    vn = sw;
   }
   __syncwarp();
 }
