@@ -54,7 +54,16 @@ typedef struct wg_instance {
   const void* D;       /* n (loop and batch kinds) */
   const void* oddV;    /* n (WG_KIND_LOOP with has_odd) */
   double oddloop[2];   /* WG_KIND_LOOP with has_odd */
+  /* Sieve terms [term_begin, term_end) of the instance's Gray-code order only (both 0: all
+   * terms).  The outputs are then that shard's share of the result, scaled like the full
+   * result, so the shards of a partition of [0, steps) sum to it: one GPU per shard and a
+   * host-side sum is the multi-GPU form of the sieve (no collective on the data path). */
+  int64_t term_begin;
+  int64_t term_end;
 } wg_instance;
+
+/* Number of sieve terms of an instance (the range that term_begin/term_end index). */
+long long wg_instance_terms(const wg_instance* inst);
 
 typedef struct wg_plan wg_plan;
 

@@ -92,6 +92,8 @@ class WgInstance(ctypes.Structure):
         ("D", ctypes.c_void_p),
         ("oddV", ctypes.c_void_p),
         ("oddloop", ctypes.c_double * 2),
+        ("term_begin", ctypes.c_int64),
+        ("term_end", ctypes.c_int64),
     ]
 
 
@@ -101,7 +103,7 @@ EXPORTS = [
     "wg_plan_kernel_launches", "wg_plan_partials", "wg_plan_chunk", "wg_plan_transfer_bytes",
     "wg_plan_destroy", "wg_run",
     "wg_measure_fp_peaks", "wg_hafnian_noalloc", "wg_state_create", "wg_state_destroy",
-    "wg_plan_create_requests", "wg_plan_device_bytes",
+    "wg_plan_create_requests", "wg_plan_device_bytes", "wg_instance_terms",
 ]
 
 
@@ -131,6 +133,8 @@ def load(build_if_needed=True):
     lib.wg_init.argtypes = [i32]
     lib.wg_last_error.restype = ctypes.c_char_p
     lib.wg_instance_outputs.argtypes = [ctypes.POINTER(WgInstance)]
+    lib.wg_instance_terms.argtypes = [ctypes.POINTER(WgInstance)]
+    lib.wg_instance_terms.restype = ctypes.c_longlong
     lib.wg_hafnian.argtypes = [vp, i32, i32, ip, i32, i32, i32, dp, vp]
     lib.wg_loop_hafnian.argtypes = [vp, vp, i32, i32, ip, i32, i32, dp, vp, i32, i32, dp, vp]
     lib.wg_loop_hafnian_batch.argtypes = [vp, vp, i32, i32, ip, i32, i32, i32, i32, i32, i32, dp, vp]
@@ -198,6 +202,25 @@ class Instance:
             z = complex(oddloop)
             s.oddloop[0], s.oddloop[1] = z.real, z.imag
         self.struct = s
+
+    def terms(self):
+        """Number of sieve terms (the range that ``shard`` partitions)."""
+        n = load().wg_instance_terms(ctypes.byref(self.struct))
+        if n < 0:
+            check(int(n))
+        return int(n)
+
+    def shard(self, begin, end):
+        """A copy restricted to sieve terms [begin, end) (non-empty); its outputs are that
+        shard's share of the result, so the shards of a partition of [0, terms()) sum to the
+        full outputs."""
+        if not 0 <= begin < end:
+            raise ValueError("a shard needs 0 <= begin < end (got [%d, %d))" % (begin, end))
+        other = Instance.__new__(Instance)
+        other.__dict__.update(self.__dict__)
+        other.struct = WgInstance.from_buffer_copy(self.struct)
+        other.struct.term_begin, other.struct.term_end = int(begin), int(end)
+        return other
 
     def outputs(self):
         if self.struct.kind == WG_KIND_BATCH_EVEN:

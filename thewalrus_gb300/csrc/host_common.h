@@ -156,20 +156,22 @@ static inline bool lb_schedule(int Ki, LbLane* lanes, LbOwner* own) {
 // Two-row steady-state schedule for K coefficients: the pieces of both rows' r-sums (each j's
 // j-1 products cut into ceil((j-1)/t) runs, per row) packed into 32 lanes, at most three pieces
 // per lane, largest first onto the least-loaded lane that fits; smallest feasible t.
-static inline bool lb_schedule2(int K, LbLane2* lanes, LbOwner2* own) {
+static inline bool lb_schedule2(int K0, int K1, LbLane2* lanes, LbOwner2* own) {
   for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
   for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
-  const int W = K * (K - 1) / 2;
+  if (K0 < 0 || K1 < K0 || K1 > LB2_KMAX) return false;
+  const int W = K0 * (K0 - 1) / 2 + K1 * (K1 - 1) / 2;
   if (W == 0) return true;
   struct Piece { int row, j, rlo, len; };
-  for (int t = std::max(1, (2 * W + 31) / 32); t <= 64; ++t) {
+  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
     int npcs = 0;
-    for (int j = 2; j <= K; ++j) npcs += 2 * ((j - 1 + t - 1) / t);
+    for (int row = 0; row < 2; ++row)
+      for (int j = 2; j <= (row ? K1 : K0); ++j) npcs += (j - 1 + t - 1) / t;
     if (npcs > 96) continue;
     Piece pcs[96];
     npcs = 0;
     for (int row = 0; row < 2; ++row)
-      for (int j = 2; j <= K; ++j) {
+      for (int j = 2; j <= (row ? K1 : K0); ++j) {
         const int x = j - 1, p = (x + t - 1) / t;
         int r = 1;
         for (int q = 0; q < p; ++q) {
@@ -215,6 +217,20 @@ static inline bool lb_schedule2(int K, LbLane2* lanes, LbOwner2* own) {
     for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
   }
   return false;
+}
+
+// every two-row table: lanes[LB2_IDS * 32], own[LB2_IDS * (LB2_KMAX + 1)], entry lb2_id(K0, K1)
+static inline bool lb_schedule2_all(LbLane2* lanes, LbOwner2* own) {
+  for (int K1 = 0; K1 <= LB2_KMAX; ++K1)
+    for (int d = 0; d <= 1; ++d) {
+      const int K0 = K1 - d, id = lb2_id(K0 < 0 ? 0 : K0, K1) + (K0 < 0 ? 1 : 0);
+      if (K0 < 0) {  // unused entry (K1 = 0, K0 = -1): empty schedule
+        lb_schedule2(0, 0, &lanes[id * 32], &own[id * (LB2_KMAX + 1)]);
+        continue;
+      }
+      if (!lb_schedule2(K0, K1, &lanes[id * 32], &own[id * (LB2_KMAX + 1)])) return false;
+    }
+  return true;
 }
 
 }  // namespace wg

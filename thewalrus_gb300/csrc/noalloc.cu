@@ -43,8 +43,8 @@ constexpr int kMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 static __device__ LbLane g_lane_tab[(LB_KMAX + 1) * 32];
 static __device__ LbOwner g_own_tab[(LB_KMAX + 1) * (LB_KMAX + 1)];
-static __device__ LbLane2 g_lane2_tab[(LB2_KMAX + 1) * 32];
-static __device__ LbOwner2 g_own2_tab[(LB2_KMAX + 1) * (LB2_KMAX + 1)];
+static __device__ LbLane2 g_lane2_tab[LB2_IDS * 32];
+static __device__ LbOwner2 g_own2_tab[LB2_IDS * (LB2_KMAX + 1)];
 
 // byte offsets inside g_scratch
 constexpr size_t kOffInst = 0;
@@ -102,10 +102,9 @@ static int setup(int dev, DeviceState** out) {
     static LbOwner own[(LB_KMAX + 1) * (LB_KMAX + 1)];
     for (int k = 0; k <= LB_KMAX; ++k)
       if (!lb_schedule(k, &lanes[k * 32], &own[k * (LB_KMAX + 1)])) return err(WG_EINVAL, "no La Budde schedule");
-    static LbLane2 lanes2[(LB2_KMAX + 1) * 32];
-    static LbOwner2 own2[(LB2_KMAX + 1) * (LB2_KMAX + 1)];
-    for (int k = 0; k <= LB2_KMAX; ++k)
-      if (!lb_schedule2(k, &lanes2[k * 32], &own2[k * (LB2_KMAX + 1)])) return err(WG_EINVAL, "no La Budde schedule");
+    static LbLane2 lanes2[LB2_IDS * 32];
+    static LbOwner2 own2[LB2_IDS * (LB2_KMAX + 1)];
+    if (!lb_schedule2_all(lanes2, own2)) return err(WG_EINVAL, "no La Budde schedule");
     if (sieve_tables_all(&binom[0][0], inv) != cudaSuccess ||
         cudaMemcpyToSymbol(g_lane_tab, lanes, sizeof(lanes)) != cudaSuccess ||
         cudaMemcpyToSymbol(g_own_tab, own, sizeof(own)) != cudaSuccess ||

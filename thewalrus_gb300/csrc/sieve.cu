@@ -92,11 +92,9 @@ static int ensure_init(int device) {
   }
   CK(cudaMemcpy(g_lb_lane, lanes.data(), sizeof(LbLane) * lanes.size(), cudaMemcpyHostToDevice));
   CK(cudaMemcpy(g_lb_own, own.data(), sizeof(LbOwner) * own.size(), cudaMemcpyHostToDevice));
-  std::vector<LbLane2> lanes2((LB2_KMAX + 1) * 32);
-  std::vector<LbOwner2> own2((LB2_KMAX + 1) * (LB2_KMAX + 1));
-  for (int k = 0; k <= LB2_KMAX; ++k)
-    if (!lb_schedule2(k, &lanes2[k * 32], &own2[k * (LB2_KMAX + 1)]))
-      return fail(WG_EINVAL, "no two-row La Budde schedule for %d coefficients", k);
+  std::vector<LbLane2> lanes2(LB2_IDS * 32);
+  std::vector<LbOwner2> own2(LB2_IDS * (LB2_KMAX + 1));
+  if (!lb_schedule2_all(lanes2.data(), own2.data())) return fail(WG_EINVAL, "no two-row La Budde schedule");
   if (!g_lb_lane2) {
     CK(cudaMalloc(&g_lb_lane2, sizeof(LbLane2) * lanes2.size()));
     CK(cudaMalloc(&g_lb_own2, sizeof(LbOwner2) * own2.size()));
@@ -117,6 +115,7 @@ struct Prepared {
   std::vector<double> scales;
   std::vector<unsigned char> ext;  // extended matrix in the kernel's scalar type (empty: formed on device)
   size_t ext_bytes = 0;
+  long long t_lo = 0, t_hi = 0;  // sieve terms [t_lo, t_hi) of this instance
 };
 
 struct Group {
@@ -304,6 +303,16 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
     steps *= R;
   }
   d.steps = steps;
+  if (in.term_begin == 0 && in.term_end == 0) {
+    P.t_lo = 0;
+    P.t_hi = steps;
+  } else {
+    if (in.term_begin < 0 || in.term_end < in.term_begin || in.term_end > steps)
+      return fail(WG_EINVAL, "term range [%lld, %lld) outside the %lld sieve terms", (long long)in.term_begin,
+                  (long long)in.term_end, steps);
+    P.t_lo = in.term_begin;
+    P.t_hi = in.term_end;
+  }
   // term matrix size bounds
   const int m_max = 2 * (int)std::count_if(reps.begin(), reps.end(), [](int r) { return r > 0; });
   P.m_max = m_max;
@@ -457,6 +466,8 @@ static int prepare_request(const wg_request& r, const wg_state& st, int precisio
     steps *= R;
   }
   d.steps = steps;
+  P.t_lo = 0;
+  P.t_hi = steps;
   int nnz = 0;
   bool all_odd = true;
   for (int i = 0; i < r.E; ++i) {
@@ -553,7 +564,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
         nser = std::max(nser, P[i].nser_need);
         narr = std::max(narr, P[i].narr);
         tile = tile && P[i].tile_ok;
-        total_cost += P[i].term_cost * (double)P[i].d.steps;
+        total_cost += P[i].term_cost * (double)(P[i].t_hi - P[i].t_lo);
       }
     G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
     const int max_smem = 227 * 1024;
@@ -570,22 +581,23 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     // chunking: about 4 chunks per resident warp (scaled), largest instances first
     const double target = std::max(1.0, total_cost / (double)(resident * 4.0 * chunk_scale));
     std::stable_sort(members.begin(), members.end(), [&](int a, int b) {
-      return P[a].term_cost * (double)P[a].d.steps > P[b].term_cost * (double)P[b].d.steps;
+      return P[a].term_cost * (double)(P[a].t_hi - P[a].t_lo) > P[b].term_cost * (double)(P[b].t_hi - P[b].t_lo);
     });
     G.chunk_begin = (int)pl->chunks.size();
     for (int i : members) {
       InstDev& d = P[i].d;
+      const long long lo = P[i].t_lo, range = P[i].t_hi - P[i].t_lo;
       long long per = (long long)std::max(1.0, std::floor(target / P[i].term_cost));
-      if (per > d.steps) per = d.steps;
-      const long long nch = (d.steps + per - 1) / per;
+      if (per > range) per = range;
+      const long long nch = range > 0 ? (range + per - 1) / per : 0;
       d.part_base = nparts;
       d.nchunks = (int)nch;
       for (long long c = 0; c < nch; ++c) {
         ChunkDev ch;
         ch.inst = i;
         ch.part = nparts + (int)c * d.nout;
-        ch.t0 = d.steps * c / nch;
-        ch.t1 = d.steps * (c + 1) / nch;
+        ch.t0 = lo + range * c / nch;
+        ch.t1 = lo + range * (c + 1) / nch;
         pl->chunks.push_back(ch);
       }
       nparts += (int)nch * d.nout;
@@ -792,6 +804,15 @@ int wg_instance_outputs(const wg_instance* in) {
   if (in->kind == WG_KIND_BATCH_EVEN) return 2 * in->batch_max + in->cutoff + 1;
   if (in->kind == WG_KIND_BATCH_ODD) return 2 * in->batch_max + in->cutoff + 2;
   return 1;
+}
+
+long long wg_instance_terms(const wg_instance* in) {
+  if (!in) return fail(WG_EINVAL, "NULL instance");
+  Prepared P;
+  wg_instance whole = *in;
+  whole.term_begin = whole.term_end = 0;
+  const int rc = prepare(whole, WG_PREC_FP64, P);
+  return rc ? (long long)rc : P.d.steps;
 }
 
 int wg_plan_create_ex(const wg_instance* inst, int count, int precision, const wg_plan_options* options,

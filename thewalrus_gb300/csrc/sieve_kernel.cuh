@@ -84,9 +84,10 @@ struct LbOwner {
 };
 constexpr int LB_KMAX = 64;
 
-// Two-row schedule (steady state, both rows with Kc coefficients, Kc <= 32): the r-sums of rows
-// i and i+1 share one pass; up to three pieces per lane, piece q of lane l in slot 3*l+q, and
-// bit q of rowmask tells which of the two rows it belongs to.
+// Two-row schedule (rows i and i+1 with K0 = min(i, Kc) and K1 = min(i+1, Kc) <= 32 coefficients,
+// so K1 - K0 is 1 in the triangle and 0 in the steady state): the r-sums of both rows share one
+// pass; up to three pieces per lane, piece q of lane l in slot 3*l+q, and bit q of rowmask tells
+// which of the two rows it belongs to.  Tables are indexed by lb2_id(K0, K1).
 struct LbLane2 {
   signed char j[3], rlo[3], len[3];
   unsigned char rowmask;
@@ -96,12 +97,14 @@ struct LbOwner2 {
   unsigned char n0, n1, s0[7], s1[7];
 };
 constexpr int LB2_KMAX = 32;
+constexpr int LB2_IDS = 2 * (LB2_KMAX + 1);
+__host__ __device__ __forceinline__ int lb2_id(int K0, int K1) { return 2 * K1 + (K1 - K0); }
 
 struct SieveParams {
   const LbLane* lb_lane;    // [(LB_KMAX+1) * 32]
   const LbOwner* lb_own;    // [(LB_KMAX+1) * (LB_KMAX+1)]
-  const LbLane2* lb_lane2;  // [(LB2_KMAX+1) * 32]
-  const LbOwner2* lb_own2;  // [(LB2_KMAX+1) * (LB2_KMAX+1)]
+  const LbLane2* lb_lane2;  // [LB2_IDS * 32]
+  const LbOwner2* lb_own2;  // [LB2_IDS * (LB2_KMAX+1)]
   const InstDev* inst;
   const ChunkDev* chunks;
   int nchunks;
@@ -375,8 +378,10 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
     return rcap;
   };
   for (int i = 1; i <= m;) {
-    if (Kc >= 2 && Kc <= LB2_KMAX && i >= Kc && i + 1 <= m) {
+    if (Kc >= 2 && Kc <= LB2_KMAX && i + 1 <= m) {
       // ---- rows i and i+1 together: both r-sums need rows <= i-1 only
+      const int K0 = i < Kc ? i : Kc, K1 = i + 1 < Kc ? i + 1 : Kc;
+      const int sid = lb2_id(K0, K1);
       const int rc0 = fill_tb(i, tb);
       const int rc1 = fill_tb(i + 1, tb + kw);
       __syncwarp();
@@ -385,7 +390,7 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
       const int c0 = prow + 1 == kw ? 0 : prow + 1;  // circular slots of rows i and i+1
       const int c1 = c0 + 1 == kw ? 0 : c0 + 1;
       {
-        const LbLane2 sc = lbl2[Kc * 32 + lane];
+        const LbLane2 sc = lbl2[sid * 32 + lane];
         const int l0 = sc.len[0], l1 = sc.len[1], l2 = sc.len[2];
         const int tot = l0 + l1 + l2;
         S acc = A::zero();
@@ -410,9 +415,9 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
       }
       __syncwarp();
       const int jj = lane + 1;
-      const LbOwner2* ow = &lbo2[Kc * (LB2_KMAX + 1) + (jj <= Kc ? jj : 0)];
-      S ci = A::zero();
-      if (jj <= Kc) {
+      const LbOwner2* ow = &lbo2[sid * (LB2_KMAX + 1) + (jj <= K1 ? jj : 0)];
+      S ci = A::zero();  // c[i][jj]: zero above row i's degree (jj = i + 1 in the triangle)
+      if (jj <= K0) {
         S val = (jj <= i - 1) ? cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj) : A::zero();
         val = A::fnma(alpha0, cw_at(W, ldw, nb, win, kw, tile, i - 1, prow, jj - 1), val);
         for (int k = 0; k < ow->n0; ++k) val = A::sub(val, part[ow->s0[k]]);
@@ -420,10 +425,10 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
       }
       S cim1 = shfl_up_s(ci, 1);  // c[i][jj-1]
       if (lane == 0) cim1 = A::one();
-      if (jj <= Kc) {
+      if (jj <= K1) {
         S v1 = A::fnma(alpha1, cim1, ci);
         for (int k = 0; k < ow->n1; ++k) v1 = A::sub(v1, part[ow->s1[k]]);
-        cw_at(W, ldw, nb, win, kw, tile, i, c0, jj) = ci;
+        if (jj <= K0) cw_at(W, ldw, nb, win, kw, tile, i, c0, jj) = ci;
         cw_at(W, ldw, nb, win, kw, tile, i + 1, c1, jj) = v1;
       }
       if (lane == 0) {
