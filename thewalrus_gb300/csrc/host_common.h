@@ -162,60 +162,50 @@ static inline bool lb_schedule2(int K0, int K1, LbLane2* lanes, LbOwner2* own) {
   if (K0 < 0 || K1 < K0 || K1 > LB2_KMAX) return false;
   const int W = K0 * (K0 - 1) / 2 + K1 * (K1 - 1) / 2;
   if (W == 0) return true;
-  struct Piece { int row, j, rlo, len; };
-  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
-    int npcs = 0;
-    for (int row = 0; row < 2; ++row)
-      for (int j = 2; j <= (row ? K1 : K0); ++j) npcs += (j - 1 + t - 1) / t;
-    if (npcs > 96) continue;
-    Piece pcs[96];
-    npcs = 0;
-    for (int row = 0; row < 2; ++row)
-      for (int j = 2; j <= (row ? K1 : K0); ++j) {
-        const int x = j - 1, p = (x + t - 1) / t;
-        int r = 1;
-        for (int q = 0; q < p; ++q) {
-          const int len = x / p + (q < x % p ? 1 : 0);
-          pcs[npcs++] = {row, j, r, len};
-          r += len;
-        }
-      }
-    for (int a = 1; a < npcs; ++a) {  // stable insertion sort, longest first
-      const Piece key = pcs[a];
-      int b = a - 1;
-      while (b >= 0 && pcs[b].len < key.len) { pcs[b + 1] = pcs[b]; --b; }
-      pcs[b + 1] = key;
-    }
-    int load[32] = {0}, nseg[32] = {0};
-    Piece seg[32][3];
-    bool ok = true;
-    for (int q = 0; q < npcs && ok; ++q) {
-      int best = -1;
-      for (int l = 0; l < 32; ++l)
-        if (nseg[l] < 3 && load[l] + pcs[q].len <= t && (best < 0 || load[l] < load[best])) best = l;
-      if (best < 0) ok = false;
-      else { seg[best][nseg[best]++] = pcs[q]; load[best] += pcs[q].len; }
-    }
-    if (!ok) continue;
-    bool fits = true;
-    for (int l = 0; l < 32 && fits; ++l) {
-      LbLane2& L = lanes[l];
-      for (int k = 0; k < nseg[l]; ++k) {
-        L.j[k] = (signed char)seg[l][k].j;
-        L.rlo[k] = (signed char)seg[l][k].rlo;
-        L.len[k] = (signed char)seg[l][k].len;
-        if (seg[l][k].row) L.rowmask |= (unsigned char)(1u << k);
-        LbOwner2& o = own[seg[l][k].j];
-        unsigned char& n = seg[l][k].row ? o.n1 : o.n0;
-        unsigned char* sl = seg[l][k].row ? o.s1 : o.s0;
-        if (n >= 7) { fits = false; break; }
-        sl[n++] = (unsigned char)(3 * l + k);
-      }
-    }
-    if (fits) return true;
-    for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
-    for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
+  // the r-sums (row, j) longest first, poured into the lanes in order: a lane closes when it
+  // holds t products or four pieces, and a sum that crosses a lane boundary is split there
+  struct Sum { int row, j, len; };
+  Sum sums[2 * (LB2_KMAX + 1)];
+  int ns = 0;
+  for (int row = 0; row < 2; ++row)
+    for (int j = 2; j <= (row ? K1 : K0); ++j) sums[ns++] = {row, j, j - 1};
+  for (int x = 1; x < ns; ++x) {  // stable insertion sort, longest first
+    const Sum key = sums[x];
+    int y = x - 1;
+    while (y >= 0 && sums[y].len < key.len) { sums[y + 1] = sums[y]; --y; }
+    sums[y + 1] = key;
   }
+  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
+    for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
+    for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
+    int lane = 0, load = 0, npc = 0;
+    bool ok = true;
+    for (int q = 0; q < ns && ok; ++q) {
+      int r = 1, left = sums[q].len;
+      while (left > 0 && ok) {
+        if (load == t || npc == 3) { ++lane; load = 0; npc = 0; }
+        if (lane >= 32) { ok = false; break; }
+        const int take = std::min(left, t - load);
+        LbLane2& L = lanes[lane];
+        L.j[npc] = (signed char)sums[q].j;
+        L.rlo[npc] = (signed char)r;
+        L.len[npc] = (signed char)take;
+        if (sums[q].row) L.rowmask |= (unsigned char)(1u << npc);
+        LbOwner2& o = own[sums[q].j];
+        unsigned char& n = sums[q].row ? o.n1 : o.n0;
+        unsigned char* sl = sums[q].row ? o.s1 : o.s0;
+        if (n >= 7) { ok = false; break; }
+        sl[n++] = (unsigned char)(3 * lane + npc);
+        ++npc;
+        load += take;
+        r += take;
+        left -= take;
+      }
+    }
+    if (ok) return true;
+  }
+  for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
+  for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
   return false;
 }
 

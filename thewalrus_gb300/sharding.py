@@ -5,9 +5,8 @@ The sieve is a sum over independent terms, so N processes (one per GPU) each eva
 kernels as ``term_begin``/``term_end``) and the shards' results are summed on the host: one
 all-reduce of a few float64 values per call after the device-to-host copy, nothing on the data
 path.  ``combine`` does that sum with ``torch.distributed`` (gloo on host tensors, NCCL on device
-tensors).  Thewalrus itself is single-process; the shard boundaries follow the scope table's
-plan for multi-GPU use of the sieve (contiguous term ranges, one scalar or one batch vector
-reduced per instance).
+tensors).  Thewalrus itself is single-process; per instance the reduction is one complex scalar
+(or one batch vector).
 """
 import numpy as np
 
