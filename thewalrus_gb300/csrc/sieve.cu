@@ -149,6 +149,11 @@ struct wg_plan {
   long long device_bytes = 0;
   bool async_alloc = false;
   cudaStream_t alloc_stream = nullptr;
+  // groups after the first run on side streams forked from the caller's stream, so that one
+  // group's persistent launch fills the SMs that another's tail leaves idle
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> side_done;
+  cudaEvent_t fork = nullptr;
 };
 
 struct wg_state {
@@ -578,8 +583,12 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     }
     G.wpc = wpc;
     const long long resident = (long long)g_num_sms * per_sm * wpc;
-    // chunking: about 4 chunks per resident warp (scaled), largest instances first
-    const double target = std::max(1.0, total_cost / (double)(resident * 4.0 * chunk_scale));
+    // chunking: about 4 chunks per resident warp (scaled), largest instances first, and no chunk
+    // above ~1000 term-equivalents of a 40-row tile (a fraction of a second of one warp), so the
+    // tail of a long batch stays short
+    constexpr double kMaxChunkCost = 6.4e7;
+    const double target =
+        std::max(1.0, std::min(total_cost / (double)(resident * 4.0 * chunk_scale), kMaxChunkCost * chunk_scale));
     std::stable_sort(members.begin(), members.end(), [&](int a, int b) {
       return P[a].term_cost * (double)(P[a].t_hi - P[a].t_lo) > P[b].term_cost * (double)(P[b].t_hi - P[b].t_lo);
     });
@@ -683,7 +692,23 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
 }
 
 static int launch_plan(wg_plan* pl, cudaStream_t st) {
-  for (size_t g = 0; g < pl->groups.size(); ++g) {
+  const size_t ng = pl->groups.size();
+  if (ng > 1) {
+    if (pl->side.size() < ng - 1) {
+      if (!pl->fork) CK(cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming));
+      while (pl->side.size() < ng - 1) {
+        cudaStream_t s2;
+        cudaEvent_t e2;
+        CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+        pl->side.push_back(s2);
+        pl->side_done.push_back(e2);
+      }
+    }
+    CK(cudaEventRecord(pl->fork, st));
+    for (size_t g = 1; g < ng; ++g) CK(cudaStreamWaitEvent(pl->side[g - 1], pl->fork, 0));
+  }
+  for (size_t g = 0; g < ng; ++g) {
     const Group& G = pl->groups[g];
     SieveParams p;
     p.lb_lane = g_lb_lane;
@@ -698,8 +723,13 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
     p.counter = pl->d_counters + g;
     p.err = pl->d_err;
     p.L = G.L;
-    const cudaError_t e = sieve_launch(G.stype, G.ns, p, G.ctas, G.wpc, st);
+    const cudaStream_t gs = g == 0 ? st : pl->side[g - 1];
+    const cudaError_t e = sieve_launch(G.stype, G.ns, p, G.ctas, G.wpc, gs);
     if (e != cudaSuccess) return fail(WG_ECUDA, "sieve launch: %s", cudaGetErrorString(e));
+    if (g > 0) {
+      CK(cudaEventRecord(pl->side_done[g - 1], gs));
+      CK(cudaStreamWaitEvent(st, pl->side_done[g - 1], 0));
+    }
   }
   const int ninst = (int)pl->inst.size();
   if (ninst > 0) {
@@ -742,6 +772,9 @@ static int execute_plan(wg_plan* pl, cudaStream_t st) {
 static void destroy_plan(wg_plan* pl) {
   if (!pl) return;
   if (pl->graph_exec) cudaGraphExecDestroy(pl->graph_exec);
+  for (cudaStream_t s2 : pl->side) cudaStreamDestroy(s2);
+  for (cudaEvent_t e2 : pl->side_done) cudaEventDestroy(e2);
+  if (pl->fork) cudaEventDestroy(pl->fork);
   if (pl->dmem) {
     if (pl->async_alloc) cudaFreeAsync(pl->dmem, pl->alloc_stream);
     else cudaFree(pl->dmem);
