@@ -464,6 +464,24 @@ def run_precision(args):
                 if name == "adjacency01" and p == "fp64":
                     assert round(g.real) == round(ref.real)
         table[name] = {p: {"max": float(np.max(v)), "median": float(np.median(v))} for p, v in errs.items()}
+    # 0/1 graphs against the exact modular oracle (integer counts): n = 32 (counts ~ 2^41) and
+    # n = 40 (~ 2^58, beyond FP64's integers)
+    exact_rows = {}
+    for n, seeds in ((32, range(args.precision_seeds)), (40, range(2))):
+        errs = {"fp64": [], "df": []}
+        rounds = 0
+        for seed in seeds:
+            A = wl.adjacency01(n, seed=seed)
+            ref = oracle.exact_hafnian(A)
+            for p in ("fp64", "df"):
+                g = tw.hafnian(A, precision=p)
+                errs[p].append(abs(complex(g) - ref) / ref)
+                if p == "fp64":
+                    rounds += int(round(g.real) == ref)
+        exact_rows["adjacency01_n%d" % n] = {
+            "seeds": len(errs["fp64"]), "fp64_rounds_exactly": rounds,
+            **{p: {"max": float(np.max(v)), "median": float(np.median(v))} for p, v in errs.items()}}
+    table["exact_integer"] = exact_rows
     timing = {}
     for name, gen in gens.items():
         A = gen(48, seed=0)
@@ -472,7 +490,7 @@ def run_precision(args):
             t0 = time.perf_counter()
             tw.hafnian(A, precision=p)
             timing["%s/%s" % (name, p)] = time.perf_counter() - t0
-    print(json.dumps({"metric": "relative error vs _Float128 oracle (n=%d, %d seeds per class)"
+    print(json.dumps({"metric": "relative error vs _Float128 oracle (n=%d, %d seeds per class) and vs exact counts (0/1 graphs)"
                       % (args.precision_n, args.precision_seeds), "errors": table,
                       "n48_seconds_per_hafnian": timing}), flush=True)
 

@@ -66,6 +66,9 @@ def _load():
             f.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
             f = getattr(lib, "oracle_charpoly" + sfx)
             f.argtypes = [dp, ctypes.c_int, dp]
+        for k in range(len(EXACT_PRIMES)):
+            f = getattr(lib, "oracle_exact_hafnian_p%d" % k)
+            f.argtypes = [ip, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int, ip]
         _lib = lib
     return _lib
 
@@ -317,6 +320,43 @@ def loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True, precision="
     assert A.shape[1] == n and D.shape[1] == n and len(fixed_reps) == n - 1
     rows = [loop_hafnian_batch(A, D[k], fixed_reps, N_cutoff, glynn, precision, nthreads) for k in range(len(D))]
     return np.array(rows, dtype=np.complex128).reshape(len(D), N_cutoff + 1)
+
+
+EXACT_PRIMES = (2147483647, 2147483629, 2147483587, 2147483579, 2147483563)
+
+
+def exact_hafnian(A, reps=None, glynn=True, nthreads=None):
+    """Exact hafnian (a Python int) of an integer-valued symmetric matrix: the sieve of
+    thewalrus/_hafnian.py:415-467 evaluated over F_p for five 31-bit primes (oracle_exact.c), then
+    the Chinese remainder theorem; exact while |haf| < 2^153."""
+    A = np.asarray(A)
+    if not np.all(np.equal(np.mod(A, 1), 0)):
+        raise ValueError("exact_hafnian needs an integer-valued matrix")
+    n = A.shape[0]
+    reps = [1] * n if reps is None else list(reps)
+    N = sum(reps)
+    if N == 0:
+        return 1
+    if N % 2:
+        return 0
+    x, edge_reps, _ = matched_reps(reps)
+    Ax = np.ascontiguousarray(A[np.ix_(x, x)].astype(np.int64))
+    r = np.ascontiguousarray(edge_reps, dtype=np.int64)
+    lib = _load()
+    res = []
+    for k, p in enumerate(EXACT_PRIMES):
+        out = ctypes.c_int64()
+        getattr(lib, "oracle_exact_hafnian_p%d" % k)(
+            Ax.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), Ax.shape[0],
+            r.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), len(r), int(bool(glynn)),
+            nthreads or _default_threads(), ctypes.byref(out))
+        res.append(int(out.value))
+    M, v = 1, 0
+    for p, a in zip(EXACT_PRIMES, res):  # CRT, incremental
+        t = ((a - v) * pow(M, -1, p)) % p
+        v += M * t
+        M *= p
+    return v - M if v > M // 2 else v
 
 
 def powertrace(H, n, precision="double"):

@@ -1,7 +1,8 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
 Compiles ``oracle_core.c`` three times, once per scalar type (double, long double, _Float128),
-into one shared library ``oracle/_build/liboracle.so``.  OpenMP threads split the sieve terms.
+and ``oracle_exact.c`` (the sieve over F_p for exact integer hafnians) into one shared library
+``oracle/_build/liboracle.so``.  OpenMP threads split the sieve terms.
 """
 import os
 import subprocess
@@ -21,7 +22,9 @@ VARIANTS = [
 def build(force=False, verbose=False):
     """Compile the oracle if its library is missing or older than its source."""
     src = os.path.join(HERE, "oracle_core.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    exact = os.path.join(HERE, "oracle_exact.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src),
+                                                                          os.path.getmtime(exact)):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     objs = []
@@ -32,6 +35,10 @@ def build(force=False, verbose=False):
                "-DOR_REAL=%s" % real, "-DSFX=%s" % sfx] + extra
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
         objs.append(obj)
+    obj = os.path.join(OUT_DIR, "oracle_exact.o")
+    cmd = ["gcc", "-O2", "-fPIC", "-fopenmp", "-std=gnu11", "-c", exact, "-o", obj]
+    procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    objs.append(obj)
     for cmd, p in procs:
         out, _ = p.communicate()
         if p.returncode != 0:

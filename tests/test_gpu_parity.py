@@ -145,3 +145,18 @@ def test_inputs_not_mutated():
     tw.hafnian(A)
     tw.hafnian(A, loop=True)
     assert np.array_equal(A, A0)
+
+
+def test_exact_integer_graphs():
+    # random 0/1 graphs against the exact modular oracle: relative error within 1e-12, and the
+    # FP64 sieve rounds to the exact perfect-matching count while the count's ulp-scaled error
+    # stays well below 0.5 (counts below 2^36; at n = 32, ~2^40, the cancellation between terms
+    # leaves errors of ~4e-13 relative, i.e. ~0.6 absolute)
+    for n, seeds in ((24, (1, 2, 3)), (28, (1, 2)), (32, (1, 2)), (36, (1,))):
+        for seed in seeds:
+            A = wl.adjacency01(n, seed=seed)
+            exact = oracle.exact_hafnian(A)
+            got = tw.hafnian(A)
+            assert abs(complex(got) - exact) <= 1e-12 * exact, (n, seed, got, exact)
+            if exact < 2 ** 36:
+                assert round(got.real) == exact and abs(got.imag) < 0.5, (n, seed, got, exact)

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import oracle
+from thewalrus_gb300 import workloads as wl
 
 T = [1, 1, 2, 4, 10, 26, 76, 232, 764, 2620, 9496]  # telephone numbers
 
@@ -118,3 +119,24 @@ def test_matched_reps_cases():
     assert x.shape == (0,) and er.shape == (0,) and odd is None
     x, er, odd = oracle.matched_reps([3])
     assert list(er) == [1] and odd == 0
+
+
+def test_exact_oracle_known_values():
+    import math
+
+    for n in (4, 8, 12, 24):
+        assert oracle.exact_hafnian(np.ones((n, n), dtype=np.int64)) == math.prod(range(n - 1, 0, -2))
+    rng = np.random.default_rng(0)
+    for n in (6, 8, 10):
+        A = wl.adjacency01(n, seed=n)
+        assert oracle.exact_hafnian(A) == round(oracle.brute_hafnian(A).real)
+        assert oracle.exact_hafnian(A, glynn=False) == round(oracle.brute_hafnian(A).real)
+        B = rng.integers(-3, 4, size=(n, n))
+        B = B + B.T
+        assert oracle.exact_hafnian(B) == round(oracle.brute_hafnian(B).real)
+    A = rng.integers(-2, 3, size=(4, 4))
+    A = A + A.T
+    assert oracle.exact_hafnian(A, reps=[2, 1, 3, 2]) == round(complex(oracle.hafnian_repeated(A, [2, 1, 3, 2])).real)
+    # against the _Float128 oracle on a 20-vertex graph
+    A = wl.adjacency01(20, seed=4)
+    assert oracle.exact_hafnian(A) == round(complex(oracle.hafnian(A, precision="quad")).real)
