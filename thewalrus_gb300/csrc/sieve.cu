@@ -573,10 +573,15 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
       }
     G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
     const int max_smem = 227 * 1024;
-    int wpc = std::min(wpc_cap, max_smem / G.L.bytes);
-    if (wpc < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
-    int per_sm = 0;
-    per_sm = sieve_occupancy(G.stype, G.ns, wpc, wpc * G.L.bytes);
+    const int wmax = std::min(wpc_cap, max_smem / G.L.bytes);
+    if (wmax < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
+    // warps per CTA: the most resident warps per SM (shared memory and registers decide how many
+    // CTAs fit), larger CTAs on ties -- e.g. 2 CTAs x 7 warps where 1 x 8 would leave room unused
+    int wpc = wmax, per_sm = sieve_occupancy(G.stype, G.ns, wmax, wmax * G.L.bytes);
+    for (int w = wmax - 1; w >= std::max(1, wmax / 2); --w) {
+      const int ps = sieve_occupancy(G.stype, G.ns, w, w * G.L.bytes);
+      if (ps * w > per_sm * wpc) { wpc = w; per_sm = ps; }
+    }
     if (per_sm < 1) {
       cudaGetLastError();
       return fail(WG_ECUDA, "sieve kernel cannot be resident (workspace %d B x %d warps)", G.L.bytes, wpc);
