@@ -160,3 +160,13 @@ def test_exact_integer_graphs():
             assert abs(complex(got) - exact) <= 1e-12 * exact, (n, seed, got, exact)
             if exact < 2 ** 36:
                 assert round(got.real) == exact and abs(got.imag) < 0.5, (n, seed, got, exact)
+
+
+def test_all_ones_exact_to_n28():
+    # (n-1)!! for the all-ones matrix rounds exactly up to n = 28 (27!! ~ 2^47.6); float64 and
+    # complex128 inputs
+    for n in (20, 24, 26, 28):
+        want = math.prod(range(n - 1, 0, -2))
+        for dt in (np.float64, np.complex128):
+            got = tw.hafnian(np.ones((n, n), dtype=dt))
+            assert round(got.real) == want and abs(got.imag) < 0.5, (n, dt, got, want)
