@@ -31,6 +31,20 @@ extern "C" {
 /* arithmetic of the sieve terms */
 #define WG_PREC_FP64 0 /* FP64 throughout */
 #define WG_PREC_DF 1   /* FP32 double-float terms; FP64 pivots, divisions and accumulation */
+/* Exact sieve of an integer-valued float64 instance modulo the prime WG_MOD_PRIME_k (entries and
+ * loop weights integers of magnitude below 2^31): every output is a residue in [0, p), returned
+ * in the real part; residues of several primes give the exact integer by the Chinese remainder
+ * theorem. */
+#define WG_PREC_MOD0 2
+#define WG_PREC_MOD1 3
+#define WG_PREC_MOD2 4
+#define WG_PREC_MOD3 5
+#define WG_PREC_MOD4 6
+#define WG_MOD_PRIME_0 2147483647u
+#define WG_MOD_PRIME_1 2147483629u
+#define WG_MOD_PRIME_2 2147483587u
+#define WG_MOD_PRIME_3 2147483579u
+#define WG_MOD_PRIME_4 2147483563u
 
 /* instance kinds for the batched interface */
 #define WG_KIND_PLAIN 0      /* _calc_hafnian */

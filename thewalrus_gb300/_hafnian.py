@@ -37,6 +37,31 @@ __all__ = [
 DEFAULT_PRECISION = "fp64"
 
 
+def _integral(inst):
+    """True when an instance's inputs are real integers the exact sieve accepts (magnitudes
+    below 2^31, edge repetitions up to 50)."""
+    if not isinstance(inst, nat.Instance) or np.iscomplexobj(inst.A):
+        return False
+    for a in (inst.A, inst.D, inst.oddV):
+        if a is not None and a.size and not (np.all(np.isfinite(a)) and np.all(a == np.round(a))
+                                             and np.max(np.abs(a)) < 2 ** 31):
+            return False
+    if inst.struct.has_odd and inst.struct.oddloop[0] != round(inst.struct.oddloop[0]):
+        return False
+    return len(inst.reps) == 0 or int(np.max(inst.reps)) <= 50
+
+
+def _auto(precision, insts):
+    """The precision of a call: the caller's, else exact for integer inputs (the sieve over
+    residues modulo 31-bit primes, so integer hafnians come back exactly, rounded once to
+    complex128), else FP64."""
+    if precision:
+        return precision
+    if insts and all(_integral(i) for i in insts) and nat.exact_primes(insts) is not None:
+        return "exact"
+    return DEFAULT_PRECISION
+
+
 def input_validation(A, rtol=1e-05, atol=1e-08):
     """Checks that ``A`` is a square, NaN-free, symmetric NumPy array (raises otherwise)."""
     if not isinstance(A, np.ndarray):
@@ -147,12 +172,14 @@ def _finish(prep, precision):
 
 def _haf(A, reps=None, glynn=True, precision=None):
     """Hafnian with optional repeated rows/columns (the reference's ``_haf``)."""
-    return _finish(prepare_hafnian(A, reps, glynn), precision or DEFAULT_PRECISION)
+    prep = prepare_hafnian(A, reps, glynn)
+    return _finish(prep, _auto(precision, [prep]))
 
 
 def loop_hafnian(A, D=None, reps=None, glynn=True, precision=None):
     """Loop hafnian with optional repeated rows/columns."""
-    return _finish(prepare_loop_hafnian(A, D, reps, glynn), precision or DEFAULT_PRECISION)
+    prep = prepare_loop_hafnian(A, D, reps, glynn)
+    return _finish(prep, _auto(precision, [prep]))
 
 
 def _closed_form(A, loop, rtol, atol):
@@ -196,7 +223,9 @@ def hafnian(A, loop=False, rtol=1e-05, atol=1e-08, approx=False, num_samples=100
     """Returns the hafnian (or loop hafnian) of a symmetric matrix.
 
     Args and results as ``thewalrus.hafnian``; ``method`` is "glynn" or "inclexcl" (the loop
-    hafnian always uses the finite-difference sieve, as in the reference).
+    hafnian always uses the finite-difference sieve, as in the reference).  ``precision``:
+    None (exact for integer-valued real inputs, FP64 otherwise), "fp64", "df" (double-float
+    terms) or "exact" (integer inputs only).
     """
     input_validation(A, rtol=rtol, atol=atol)
     glynn = _method_glynn(method) if not loop else True
@@ -278,7 +307,7 @@ def prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True):
 def loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True, precision=None):
     """Loop hafnians for every photon number 0..N_cutoff of the last mode, in one sieve."""
     prep = prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn)
-    return nat.run([prep], precision or DEFAULT_PRECISION)
+    return nat.run([prep], _auto(precision, [prep]))
 
 
 def prepare_loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True):
@@ -303,7 +332,7 @@ def loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True, precision=N
     preps = prepare_loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn)
     if not preps:
         return np.zeros((0, N_cutoff + 1), dtype=np.complex128)
-    vals = nat.run(preps, precision or DEFAULT_PRECISION)
+    vals = nat.run(preps, _auto(precision, preps))
     return vals.reshape(len(preps), -1)
 
 
@@ -331,7 +360,7 @@ def hafnian_batch(matrices, loop=False, rtol=1e-05, atol=1e-08, method="glynn", 
         else:
             results[i] = prep
     if insts:
-        vals = nat.run(insts, precision or DEFAULT_PRECISION)
+        vals = nat.run(insts, _auto(precision, insts))
         for i, v in zip(where, vals):
             results[i] = np.complex128(v)
     return results

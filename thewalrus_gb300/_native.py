@@ -15,15 +15,19 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwalrus_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
-SOURCES = ["sieve.cu", "noalloc.cu", "kernels_c64.cu", "kernels_cdf.cu", "kernels_f64.cu", "kernels_fdf.cu"]
+SOURCES = ["sieve.cu", "noalloc.cu", "kernels_c64.cu", "kernels_cdf.cu", "kernels_f64.cu", "kernels_fdf.cu",
+           "kernels_mod0.cu", "kernels_mod1.cu", "kernels_mod2.cu", "kernels_mod3.cu", "kernels_mod4.cu"]
 DEPS = SOURCES + ["sieve_kernel.cuh", "arith.cuh", "host_common.h", "kernels.h", "kernels_unit.cuh"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-shared"]
 
 WG_FLOAT64, WG_COMPLEX128 = 0, 1
 WG_PREC_FP64, WG_PREC_DF = 0, 1
+WG_PREC_MOD = (2, 3, 4, 5, 6)
+MOD_PRIMES = (2147483647, 2147483629, 2147483587, 2147483579, 2147483563)
 WG_KIND_PLAIN, WG_KIND_LOOP, WG_KIND_BATCH_EVEN, WG_KIND_BATCH_ODD = 0, 1, 3, 4
 PRECISIONS = {"fp64": WG_PREC_FP64, "df": WG_PREC_DF}
+PRECISIONS.update({"mod%d" % k: v for k, v in enumerate(WG_PREC_MOD)})
 
 _lock = threading.Lock()
 _lib = None
@@ -203,6 +207,28 @@ class Instance:
             s.oddloop[0], s.oddloop[1] = z.real, z.imag
         self.struct = s
 
+    def log2_bound(self):
+        """log2 of a bound on |output|: the expanded matrix (each edge end repeated rep times,
+        loop weights on the diagonal) has haf^2 <= per <= prod of absolute row sums."""
+        s = self.struct
+        n = self.A.shape[0] if self.A.ndim == 2 else 0
+        if n == 0:
+            return 0.0
+        reps = list(self.reps)
+        if s.kind in (WG_KIND_BATCH_EVEN, WG_KIND_BATCH_ODD):  # the batch ends carry batch_max + cutoff
+            extra = [s.batch_max + s.cutoff + 1] + ([1] if s.kind == WG_KIND_BATCH_ODD else [])
+            reps = extra + reps
+        E = len(reps)
+        mult = np.array([reps[i % E] for i in range(n)], dtype=np.float64) if E else np.ones(n)
+        absA = np.abs(np.real(self.A)) + np.abs(np.imag(self.A))
+        rows = absA @ mult
+        if self.D is not None:
+            rows = rows + np.abs(self.D)
+        if s.has_odd and self.oddV is not None:
+            rows = rows + np.abs(self.oddV) + abs(complex(s.oddloop[0], s.oddloop[1]))
+        rows = np.maximum(rows, 1.0)
+        return float(0.5 * np.sum(mult * np.log2(rows))) + 1.0
+
     def terms(self):
         """Number of sieve terms (the range that ``shard`` partitions)."""
         n = load().wg_instance_terms(ctypes.byref(self.struct))
@@ -342,8 +368,43 @@ class Plan:
             pass
 
 
+def crt(residues, primes=MOD_PRIMES):
+    """The integer in (-M/2, M/2], M = prod(primes), with the given residues."""
+    M, v = 1, 0
+    for p, a in zip(primes, residues):
+        t = ((int(a) - v) * pow(M, -1, p)) % p
+        v += M * t
+        M *= p
+    return v - M if v > M // 2 else v
+
+
+def exact_primes(instances):
+    """How many of the 31-bit primes an exact run needs: enough that the product exceeds twice
+    a bound on every output's magnitude, |haf(A)| <= sqrt(prod_i r_i) with r_i the absolute row
+    sums of the expanded matrix (haf^2 <= per <= product of row sums); None beyond five."""
+    bits = 0.0
+    for inst in instances:
+        bits = max(bits, inst.log2_bound())
+    k = int(np.ceil((bits + 2.0) / 30.99))
+    return max(k, 2) if k <= len(MOD_PRIMES) else None
+
+
+def run_exact(instances, stream=0, nprimes=None):
+    """Exact outputs (Python ints) of integer-valued real instances: the sieve modulo 31-bit
+    primes on the GPU (as many as ``exact_primes`` asks), combined by the Chinese remainder
+    theorem."""
+    k = nprimes or exact_primes(instances)
+    if k is None:
+        raise ValueError("exact precision: the outputs may exceed 2^153, beyond five primes")
+    per_prime = [run(instances, "mod%d" % j, stream).real for j in range(k)]
+    return [crt([round(float(r[i])) for r in per_prime], MOD_PRIMES[:k]) for i in range(len(per_prime[0]))]
+
+
 def run(instances, precision="fp64", stream=0):
-    """Run instances through one plan; returns the concatenated complex outputs."""
+    """Run instances through one plan; returns the concatenated complex outputs.  With
+    ``precision="exact"`` the exact integers, rounded to complex128."""
+    if precision == "exact":
+        return np.array([complex(float(v), 0.0) for v in run_exact(instances, stream)], dtype=np.complex128)
     lib = load()
     insts = list(instances)
     arr = (WgInstance * max(len(insts), 1))()

@@ -1,8 +1,9 @@
 // Scalar arithmetic for the sieve kernels.
 //
-// Four scalar types share one interface (struct Ar<S>):
+// Five scalar types share one interface (struct Ar<S>):
 //   double  real FP64                 c64  complex FP64
 //   dfr     real double-float (FP32)  cdf  complex double-float
+//   modp<P> residues modulo a 31-bit prime P (exact integer sieves; integer pipe only)
 // A double-float value is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), giving
 // a 48-bit significand from FP32 instructions only.  Products use the FMA error-free
 // transformation (err = fma(a, b, -a*b)); sums use Knuth's two-sum.  Conversions to and from
@@ -128,6 +129,7 @@ struct Ar<double> {
   static constexpr int NC = 1;
   static constexpr bool cplx = false;
   static constexpr bool fp64 = true;
+  static constexpr bool modular = false;
   __device__ static __forceinline__ S zero() { return 0.0; }
   __device__ static __forceinline__ S one() { return 1.0; }
   __device__ static __forceinline__ S add(S a, S b) { return a + b; }
@@ -158,6 +160,7 @@ struct Ar<c64> {
   static constexpr int NC = 2;
   static constexpr bool cplx = true;
   static constexpr bool fp64 = true;
+  static constexpr bool modular = false;
   __device__ static __forceinline__ S zero() { return {0.0, 0.0}; }
   __device__ static __forceinline__ S one() { return {1.0, 0.0}; }
   __device__ static __forceinline__ S add(S a, S b) { return {a.re + b.re, a.im + b.im}; }
@@ -206,6 +209,7 @@ struct Ar<dfr> {
   static constexpr int NC = 1;
   static constexpr bool cplx = false;
   static constexpr bool fp64 = false;
+  static constexpr bool modular = false;
   __device__ static __forceinline__ S zero() { return {0.f, 0.f}; }
   __device__ static __forceinline__ S one() { return {1.f, 0.f}; }
   __device__ static __forceinline__ S add(S a, S b) { return df_add(a, b); }
@@ -240,6 +244,7 @@ struct Ar<cdf> {
   static constexpr int NC = 2;
   static constexpr bool cplx = true;
   static constexpr bool fp64 = false;
+  static constexpr bool modular = false;
   __device__ static __forceinline__ S zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
   __device__ static __forceinline__ S one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
   __device__ static __forceinline__ S add(S a, S b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
@@ -285,6 +290,72 @@ struct Ar<cdf> {
     return {{__shfl_sync(0xffffffffu, v.re.hi, src), __shfl_sync(0xffffffffu, v.re.lo, src)},
             {__shfl_sync(0xffffffffu, v.im.hi, src), __shfl_sync(0xffffffffu, v.im.lo, src)}};
   }
+};
+
+
+// ---------------------------------------------------------------- residues modulo a prime
+// Exact arithmetic for integer inputs: every step of the sieve (elimination with any nonzero
+// pivot, La Budde, the series, the prefactors) is a field operation, so the sieve of an integer
+// matrix is exact in F_P; the host combines three primes by the Chinese remainder theorem.
+// Products of two residues fit 62 bits and are reduced by the compile-time constant P.
+template <uint32_t P>
+struct modp {
+  uint32_t v;
+};
+
+template <uint32_t P>
+struct Ar<modp<P>> {
+  using S = modp<P>;
+  using Comp = modp<P>;
+  static constexpr int NC = 1;
+  static constexpr bool cplx = false;
+  static constexpr bool fp64 = true;  // exact zero tests, normalised (unit-subdiagonal) elimination
+  static constexpr bool modular = true;
+  __device__ static __forceinline__ S mk(uint64_t x) { return S{(uint32_t)(x % P)}; }
+  __device__ static __forceinline__ S zero() { return S{0u}; }
+  __device__ static __forceinline__ S one() { return S{1u}; }
+  __device__ static __forceinline__ S add(S a, S b) {
+    const uint32_t s = a.v + b.v;  // < 2^32
+    return S{s >= P ? s - P : s};
+  }
+  __device__ static __forceinline__ S sub(S a, S b) { return S{a.v >= b.v ? a.v - b.v : a.v + P - b.v}; }
+  __device__ static __forceinline__ S neg(S a) { return S{a.v ? P - a.v : 0u}; }
+  __device__ static __forceinline__ S mul(S a, S b) { return mk((uint64_t)a.v * b.v); }
+  __device__ static __forceinline__ S fma(S a, S b, S c) { return mk((uint64_t)a.v * b.v + c.v); }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) { return mk((uint64_t)a.v * (P - b.v) + c.v); }
+  __device__ static __forceinline__ S conj(S a) { return a; }
+  // exact for the integers and half-integers the kernel scales by
+  __device__ static __forceinline__ S of_int(long long k) {
+    const long long r = k % (long long)P;
+    return S{(uint32_t)(r < 0 ? r + P : r)};
+  }
+  __device__ static __forceinline__ S half() { return S{(P + 1) / 2}; }
+  __device__ static __forceinline__ S scale(S a, double s) {
+    const long long t = __double2ll_rn(2.0 * s);
+    return mul(mul(a, of_int(t)), half());
+  }
+  __device__ static __forceinline__ S pow(S a, uint32_t e) {
+    S r = one();
+    while (e) {
+      if (e & 1u) r = mul(r, a);
+      a = mul(a, a);
+      e >>= 1;
+    }
+    return r;
+  }
+  __device__ static __forceinline__ S recip(S a) { return pow(a, P - 2); }  // Fermat
+  __device__ static __forceinline__ S inv_int(int k) { return recip(of_int(k)); }
+  // residues travel through FP64 slots exactly (< 2^31)
+  __device__ static __forceinline__ S from_c64(c64 z) { return of_int(__double2ll_rn(z.re)); }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {(double)a.v, 0.0}; }
+  __device__ static __forceinline__ unsigned long long key(S a) { return a.v; }  // any nonzero pivot
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long) { return 0ull; }
+  __device__ static __forceinline__ bool is_zero(S a) { return a.v == 0u; }
+  __device__ static __forceinline__ Comp comp(const S& a, int) { return a; }
+  __device__ static __forceinline__ void set_comp(S& a, int, Comp v) { a = v; }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return add(a, b); }
+  __device__ static __forceinline__ Comp shfl_xor(Comp a, int m) { return S{__shfl_xor_sync(0xffffffffu, a.v, m)}; }
+  __device__ static __forceinline__ S shfl(S a, int src) { return S{__shfl_sync(0xffffffffu, a.v, src)}; }
 };
 
 }  // namespace wg

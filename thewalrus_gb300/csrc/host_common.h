@@ -16,8 +16,14 @@ static inline int sieve_occupancy(int stype, int ns, int wpc, int smem);
 static inline cudaError_t sieve_tables_all(const double* binom, const double* inv);
 
 // scalar classes
-enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3 };
-static size_t stype_bytes(int st) { return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16; }
+enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3, ST_MOD0 = 4, ST_MOD1 = 5, ST_MOD2 = 6,
+             ST_MOD3 = 7, ST_MOD4 = 8 };
+static inline bool stype_mod(int st) { return st >= ST_MOD0; }
+static size_t stype_bytes(int st) {
+  if (stype_mod(st)) return 4;
+  return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16;
+}
+static const uint32_t MOD_PRIMES[5] = {2147483647u, 2147483629u, 2147483587u, 2147483579u, 2147483563u};
 
 // register classes: rows of the term tile per row lane (8 row lanes).  Row slots beyond the
 // tile are skipped by a warp-uniform branch, so a class larger than needed costs registers, not
@@ -41,7 +47,12 @@ static inline cudaError_t sieve_launch(int stype, int ns, const SieveParams& p, 
     case ST_CPLX64: return sieve_launch_c64(ns, p, ctas, wpc, st);
     case ST_CPLXDF: return sieve_launch_cdf(ns, p, ctas, wpc, st);
     case ST_REAL64: return sieve_launch_f64(ns, p, ctas, wpc, st);
-    default: return sieve_launch_fdf(ns, p, ctas, wpc, st);
+    case ST_REALDF: return sieve_launch_fdf(ns, p, ctas, wpc, st);
+    case ST_MOD0: return sieve_launch_mod0(ns, p, ctas, wpc, st);
+    case ST_MOD1: return sieve_launch_mod1(ns, p, ctas, wpc, st);
+    case ST_MOD2: return sieve_launch_mod2(ns, p, ctas, wpc, st);
+    case ST_MOD3: return sieve_launch_mod3(ns, p, ctas, wpc, st);
+    default: return sieve_launch_mod4(ns, p, ctas, wpc, st);
   }
 }
 
@@ -50,7 +61,12 @@ static inline int sieve_occupancy(int stype, int ns, int wpc, int smem) {
     case ST_CPLX64: return sieve_occupancy_c64(ns, wpc, smem);
     case ST_CPLXDF: return sieve_occupancy_cdf(ns, wpc, smem);
     case ST_REAL64: return sieve_occupancy_f64(ns, wpc, smem);
-    default: return sieve_occupancy_fdf(ns, wpc, smem);
+    case ST_REALDF: return sieve_occupancy_fdf(ns, wpc, smem);
+    case ST_MOD0: return sieve_occupancy_mod0(ns, wpc, smem);
+    case ST_MOD1: return sieve_occupancy_mod1(ns, wpc, smem);
+    case ST_MOD2: return sieve_occupancy_mod2(ns, wpc, smem);
+    case ST_MOD3: return sieve_occupancy_mod3(ns, wpc, smem);
+    default: return sieve_occupancy_mod4(ns, wpc, smem);
   }
 }
 
@@ -59,6 +75,11 @@ static inline cudaError_t sieve_tables_all(const double* binom, const double* in
   if (e == cudaSuccess) e = sieve_tables_cdf(binom, inv);
   if (e == cudaSuccess) e = sieve_tables_f64(binom, inv);
   if (e == cudaSuccess) e = sieve_tables_fdf(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_mod0(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_mod1(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_mod2(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_mod3(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_mod4(binom, inv);
   return e;
 }
 

@@ -1,6 +1,6 @@
 // Body of one kernel translation unit: define WG_UNIT_SCALAR (the scalar type), WG_UNIT_NAME (the
-// suffix of the entry points) and WG_UNIT_CLASSES(X) (X(ns) for every register class), then
-// include this file.
+// suffix of the entry points), WG_UNIT_CLASSES(X) (X(ns) for every register class) and, for the
+// residue types, WG_UNIT_PRIME, then include this file.
 #include "kernels.h"
 
 namespace wg {
@@ -53,7 +53,17 @@ int WG_CAT(sieve_occupancy_, WG_UNIT_NAME)(int ns, int wpc, int smem) {
 cudaError_t WG_CAT(sieve_tables_, WG_UNIT_NAME)(const double* binom, const double* inv) {
   cudaError_t e = cudaMemcpyToSymbol(c_binom, binom, sizeof(c_binom));
   if (e != cudaSuccess) return e;
-  return cudaMemcpyToSymbol(c_inv, inv, sizeof(c_inv));
+  e = cudaMemcpyToSymbol(c_inv, inv, sizeof(c_inv));
+#ifdef WG_UNIT_PRIME
+  if (e != cudaSuccess) return e;
+  uint32_t invmod[256];  // 1/k mod p by k * inv(k) = 1: inv(k) = -(p / k) inv(p mod k)
+  invmod[0] = 0;
+  invmod[1] = 1;
+  const uint64_t P = WG_UNIT_PRIME;
+  for (uint64_t k = 2; k < 256; ++k) invmod[k] = (uint32_t)((P - (P / k) * invmod[P % k] % P) % P);
+  e = cudaMemcpyToSymbol(c_invmod, invmod, sizeof(invmod));
+#endif
+  return e;
 }
 
 #undef WG_CAT

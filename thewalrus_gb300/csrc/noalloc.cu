@@ -234,7 +234,7 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   const cudaError_t e = sieve_launch(st, ns, p, ctas, wpc, s);
   if (e != cudaSuccess) return err(WG_ECUDA, "sieve kernel launch failed");
   reduce_kernel<<<1, 32, 0, s>>>(p.inst, 1, p.partials, reinterpret_cast<const double*>(scr + kOffScale),
-                                 reinterpret_cast<double2*>(out_dev), p.counter, 1, 1);
+                                 reinterpret_cast<double2*>(out_dev), p.counter, 1, 1, 0u);
   if (cudaGetLastError() != cudaSuccess) return err(WG_ECUDA, "reduction kernel launch failed");
   return WG_OK;
 }

@@ -169,6 +169,13 @@ namespace wg {
 
 
 static inline void put_scalar(unsigned char* dst, int st, double re, double im) {
+  if (stype_mod(st)) {  // residue of an integer below 2^31 in magnitude (checked in prepare)
+    const long long p = (long long)MOD_PRIMES[st - ST_MOD0];
+    long long r = (long long)re % p;
+    const uint32_t v = (uint32_t)(r < 0 ? r + p : r);
+    memcpy(dst, &v, 4);
+    return;
+  }
   switch (st) {
     case ST_REAL64: memcpy(dst, &re, 8); break;
     case ST_CPLX64: memcpy(dst, &re, 8); memcpy(dst + 8, &im, 8); break;
@@ -184,6 +191,17 @@ static inline void put_scalar(unsigned char* dst, int st, double re, double im) 
       break;
     }
   }
+}
+
+static inline bool prec_mod(int precision) { return precision >= WG_PREC_MOD0 && precision <= WG_PREC_MOD4; }
+
+// 2^-e as the output scale: the FP64 value, or (modular precisions) the residue of 2^-e mod p
+static inline double pow2_scale(int e, int precision) {
+  if (!prec_mod(precision)) return std::ldexp(1.0, -e);
+  const uint64_t p = MOD_PRIMES[precision - WG_PREC_MOD0], half = (p + 1) / 2;
+  uint64_t r = 1;
+  for (int i = 0; i < e; ++i) r = r * half % p;
+  return (double)r;
 }
 
 static inline void get_val(const void* p, int dtype, size_t idx, double& re, double& im) {
@@ -264,14 +282,14 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
     d.Nodd = 0;
     d.half_first = d.glynn;
     const int e = d.glynn ? d.N / 2 - 1 : 0;
-    P.scales.push_back(std::ldexp(1.0, -e) * std::pow(alpha, -0.5 * d.N));
+    P.scales.push_back(pow2_scale(e, precision) * std::pow(alpha, -0.5 * d.N));
   } else if (kind == KIND_LOOP_ODD) {
     d.N = (int)(2 * sumr + 1);
     d.K = d.N / 2;
     d.Nodd = d.N;
     d.half_first = 0;
     const int e = d.glynn ? d.N / 2 : 0;
-    P.scales.push_back(std::ldexp(1.0, -e) * std::pow(alpha, -0.5 * d.N));
+    P.scales.push_back(pow2_scale(e, precision) * std::pow(alpha, -0.5 * d.N));
     d.oddloop = {in.oddloop[0] * salpha, in.oddloop[1] * salpha};
   } else {
     const bool odd = kind == KIND_BATCH_ODD;
@@ -295,7 +313,7 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
     }
     for (int o = 0; o < nout; ++o) {
       const int x = Nf + o;
-      P.scales.push_back((d.glynn ? std::ldexp(1.0, -(x / 2)) : 1.0) * std::pow(alpha, -0.5 * x));
+      P.scales.push_back(pow2_scale(d.glynn ? x / 2 : 0, precision) * std::pow(alpha, -0.5 * x));
     }
   }
   d.nout = nout;
@@ -338,7 +356,24 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
   if (P.kc_max > 64) return fail(WG_EINVAL, "more than 64 characteristic coefficients");
   if (d.Nodd > 250 || d.K > 250) return fail(WG_EINVAL, "photon number above the supported 250");
   const bool cplx = in.dtype == WG_COMPLEX128;
-  P.stype = precision == WG_PREC_DF ? (cplx ? ST_CPLXDF : ST_REALDF) : (cplx ? ST_CPLX64 : ST_REAL64);
+  if (prec_mod(precision)) {
+    // exact sieve: integer-valued real inputs below 2^31, binomial products exact in FP64 slots
+    if (cplx) return fail(WG_EINVAL, "exact precision needs float64 (real) inputs");
+    auto integral = [](double v) { return std::isfinite(v) && v == std::floor(v) && std::fabs(v) < 2147483648.0; };
+    for (size_t i = 0; i < (size_t)in.n * in.n; ++i)
+      if (!integral(((const double*)in.A)[i])) return fail(WG_EINVAL, "exact precision needs integer matrix entries below 2^31");
+    if (in.D)
+      for (int i = 0; i < in.n; ++i)
+        if (!integral(((const double*)in.D)[i])) return fail(WG_EINVAL, "exact precision needs integer loop weights below 2^31");
+    if (in.oddV)
+      for (int i = 0; i < in.n; ++i)
+        if (!integral(((const double*)in.oddV)[i])) return fail(WG_EINVAL, "exact precision needs integer entries below 2^31");
+    if (kind == KIND_LOOP_ODD && !integral(in.oddloop[0])) return fail(WG_EINVAL, "exact precision needs an integer self-loop weight");
+    if (maxr > 50) return fail(WG_EINVAL, "exact precision supports edge repetitions up to 50");
+    P.stype = ST_MOD0 + (precision - WG_PREC_MOD0);
+  } else {
+    P.stype = precision == WG_PREC_DF ? (cplx ? ST_CPLXDF : ST_REALDF) : (cplx ? ST_CPLX64 : ST_REAL64);
+  }
   // extended matrix [[A, D], [D^T, 0], [oddV, 0], [oddV0, 0]]  ((n+3) x (n+1))
   const int n = in.n, lda = n + 1;
   const size_t sb = stype_bytes(P.stype);
@@ -503,7 +538,8 @@ static int prepare_request(const wg_request& r, const wg_state& st, int precisio
 
 static int build_plan(const wg_instance* v, int count, int precision, const wg_plan_options& opt, wg_plan* pl) {
   if (count < 0 || (count > 0 && !v)) return fail(WG_EINVAL, "bad instance list");
-  if (precision != WG_PREC_FP64 && precision != WG_PREC_DF) return fail(WG_EINVAL, "unknown precision %d", precision);
+  if (precision != WG_PREC_FP64 && precision != WG_PREC_DF && !prec_mod(precision))
+    return fail(WG_EINVAL, "unknown precision %d", precision);
   std::vector<Prepared> P(count);
   for (int i = 0; i < count; ++i) {
     int rc = prepare(v[i], precision, P[i]);
@@ -740,8 +776,9 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
   if (ninst > 0) {
     const int threads = 128;
     const int blocks = (pl->total_out * 32 + threads - 1) / threads;  // one warp per output
+    const unsigned int modp = prec_mod(pl->precision) ? MOD_PRIMES[pl->precision - WG_PREC_MOD0] : 0u;
     reduce_kernel<<<std::max(blocks, 1), threads, 0, st>>>(pl->d_inst, ninst, pl->d_partials, pl->d_scales, pl->d_out,
-                                                           pl->d_counters, (int)pl->groups.size(), pl->total_out);
+                                                           pl->d_counters, (int)pl->groups.size(), pl->total_out, modp);
     CK(cudaGetLastError());
   }
   return WG_OK;

@@ -120,13 +120,30 @@ static __constant__ double c_binom[BINOM_N][BINOM_N];
 static __constant__ double c_inv[256];  // c_inv[k] = 1/k (k >= 1)
 
 __device__ __forceinline__ double inv_int(int k) { return k < 256 ? c_inv[k] : 1.0 / (double)k; }
+// 1/k modulo the prime of this translation unit's modular kernels (k < 256)
+static __constant__ uint32_t c_invmod[256];
+
+template <class S>
+__device__ __forceinline__ S inv_of(int k) {  // 1/k in the scalar type (k >= 1)
+  using A = Ar<S>;
+  if constexpr (A::modular) return k < 256 ? S{c_invmod[k]} : A::inv_int(k);
+  else return A::scale(A::one(), inv_int(k));
+}
+
+template <class S>
+__device__ __forceinline__ S half_of(S x) {
+  using A = Ar<S>;
+  if constexpr (A::modular) return A::mul(x, A::half());
+  else return A::scale(x, 0.5);
+}
 
 template <class S>
 __device__ __forceinline__ S scale_int(S x, int d) {
   using A = Ar<S>;
   if (d == 1) return x;
   if (d == -1) return A::neg(x);
-  return A::scale(x, (double)d);
+  if constexpr (A::modular) return A::mul(x, A::of_int(d));
+  else return A::scale(x, (double)d);
 }
 
 template <class S>
@@ -146,6 +163,10 @@ __device__ __forceinline__ S warp_sum(S v) {
 __device__ __forceinline__ double shfl_up_c(double v, int off) { return __shfl_up_sync(0xffffffffu, v, off); }
 __device__ __forceinline__ dfr shfl_up_c(dfr v, int off) {
   return {__shfl_up_sync(0xffffffffu, v.hi, off), __shfl_up_sync(0xffffffffu, v.lo, off)};
+}
+template <uint32_t P>
+__device__ __forceinline__ modp<P> shfl_up_c(modp<P> v, int off) {
+  return {__shfl_up_sync(0xffffffffu, v.v, off)};
 }
 template <class S>
 __device__ __forceinline__ S shfl_up_s(S v, int off) {
@@ -504,8 +525,14 @@ __device__ void inv_sqrt_series(const S* __restrict__ cpoly, int Kc, S* __restri
     const S gk = g[k];
     const int hi = (k + Kc) < G ? (k + Kc) : G;
     for (int n = k + 1 + lane; n <= hi; n += 32) {
-      S acc = A::fma(cpoly[n - k], A::scale(gk, 0.5 * (double)(n + k)), g[n]);
-      if (n == k + 1) acc = A::scale(acc, -inv_int(n));
+      S acc;
+      if constexpr (A::modular) {
+        acc = A::fma(cpoly[n - k], A::mul(gk, A::mul(A::of_int(n + k), A::half())), g[n]);
+        if (n == k + 1) acc = A::neg(A::mul(acc, inv_of<S>(n)));
+      } else {
+        acc = A::fma(cpoly[n - k], A::scale(gk, 0.5 * (double)(n + k)), g[n]);
+        if (n == k + 1) acc = A::scale(acc, -inv_int(n));
+      }
       g[n] = acc;
     }
     __syncwarp();
@@ -524,8 +551,14 @@ __device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, in
     const S ek = e[k];
     const int hi = (k + Q) < G ? (k + Q) : G;
     for (int n = k + 1 + lane; n <= hi; n += 32) {
-      S acc = A::fma(A::scale(q[n - k], (double)(n - k)), ek, e[n]);
-      if (n == k + 1) acc = A::scale(acc, inv_int(n));
+      S acc;
+      if constexpr (A::modular) {
+        acc = A::fma(A::mul(q[n - k], A::of_int(n - k)), ek, e[n]);
+        if (n == k + 1) acc = A::mul(acc, inv_of<S>(n));
+      } else {
+        acc = A::fma(A::scale(q[n - k], (double)(n - k)), ek, e[n]);
+        if (n == k + 1) acc = A::scale(acc, inv_int(n));
+      }
       e[n] = acc;
     }
     __syncwarp();
@@ -669,6 +702,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       }
     }
     double s_re = 0, s_im = 0, k_re = 0, k_im = 0;  // lane o: Neumaier sum of output o
+    S macc = A::zero();                               // modular kinds: lane o's residue sum
 
     for (long long t = ch.t0; t < ch.t1; ++t) {
       if (t != ch.t0) {  // Gray step: least significant digit that can move in its direction
@@ -690,11 +724,36 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       for (int off = 16; off; off >>= 1) ksum += __shfl_xor_sync(0xffffffffu, ksum, off);
       const bool batch = kind >= KIND_BATCH_EVEN;
       double bin = 1.0;
+      S binm = A::one();  // modular kinds: the binomial product as a residue (exact)
       if (!I.unit_binoms) {
         bin = (lane < E && !(batch && lane == 0)) ? c_binom[rep][g] : 1.0;
+        if constexpr (A::modular) {
+          binm = A::of_int((long long)bin);
 #pragma unroll
-        for (int off = 16; off; off >>= 1) bin *= __shfl_xor_sync(0xffffffffu, bin, off);
+          for (int off = 16; off; off >>= 1) binm = A::mul(binm, A::shfl_xor(binm, off));
+        } else {
+#pragma unroll
+          for (int off = 16; off; off >>= 1) bin *= __shfl_xor_sync(0xffffffffu, bin, off);
+        }
       }
+      // prefactor x term into the lane's sum: parity gives the sign, halve the Glynn halving
+      // of the delta_0 = 0 term, binx an extra binomial (batch outputs)
+      auto accum = [&](int parity, bool halve, S f, double binx) {
+        if constexpr (A::modular) {
+          S t = A::mul(binm, f);
+          if (binx != 1.0) t = A::mul(t, A::of_int((long long)binx));
+          if (parity) t = A::neg(t);
+          if (halve) t = A::mul(t, A::half());
+          macc = A::add(macc, t);
+        } else {
+          double pre = binx * bin;
+          if (parity) pre = -pre;
+          if (halve) pre *= 0.5;
+          const c64 z = A::to_c64(f);
+          neumaier(s_re, k_re, pre * z.re);
+          neumaier(s_im, k_im, pre * z.im);
+        }
+      };
       const int g0 = __shfl_sync(0xffffffffu, g, 0);
       const int g1 = __shfl_sync(0xffffffffu, g, 1);
       const int d0 = __shfl_sync(0xffffffffu, delta, 0);
@@ -736,18 +795,12 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
 
       if (kind == KIND_PLAIN) {
-        if (lane == 0) {
-          double pre = ((I.N / 2 - ksum) & 1) ? -bin : bin;
-          if (glynn && d0 == 0) pre *= 0.5;
-          const c64 f = A::to_c64(gser[I.K]);
-          neumaier(s_re, k_re, pre * f.re);
-          neumaier(s_im, k_im, pre * f.im);
-        }
+        if (lane == 0) accum((I.N / 2 - ksum) & 1, glynn && d0 == 0, gser[I.K], 1.0);
       } else {
         const int T = I.K;
         // even series: q_l = lam_l / 2, e = exp(q), f_even[h] = sum_t g_t e_{h-t}
         if (kind == KIND_LOOP || kind == KIND_BATCH_EVEN || kind == KIND_BATCH_ODD) {
-          for (int l = lane; l <= T; l += 32) qv[l] = l ? A::scale(lam[l], 0.5) : A::zero();
+          for (int l = lane; l <= T; l += 32) qv[l] = l ? half_of<S>(lam[l]) : A::zero();
           __syncwarp();
           exp_series<S>(qv, T, eser, T);
         }
@@ -755,13 +808,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
           S part = A::zero();
           for (int tq = lane; tq <= T; tq += 32) part = A::fma(gser[tq], eser[T - tq], part);
           part = warp_sum(part);
-          if (lane == 0) {
-            double pre = ((I.N / 2 - ksum) & 1) ? -bin : bin;
-            if (glynn && d0 == 0) pre *= 0.5;
-            const c64 f = A::to_c64(part);
-            neumaier(s_re, k_re, pre * f.re);
-            neumaier(s_im, k_im, pre * f.im);
-          }
+          if (lane == 0) accum((I.N / 2 - ksum) & 1, glynn && d0 == 0, part, 1.0);
         } else {
           // odd series in zeta: q'_1 = oddloop, q'_{2l} = lam_l/2, q'_{2l+1} = mu_l
           const int No = I.Nodd;
@@ -770,7 +817,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
             S q;
             if (l == 0) q = A::zero();
             else if (l == 1) q = A::from_c64(I.oddloop);
-            else if ((l & 1) == 0) q = (l / 2 <= T) ? A::scale(lam[l / 2], 0.5) : A::zero();
+            else if ((l & 1) == 0) q = (l / 2 <= T) ? half_of<S>(lam[l / 2]) : A::zero();
             else q = ((l - 1) / 2 <= T) ? mu[(l - 1) / 2] : A::zero();
             qv[l] = q;
           }
@@ -780,12 +827,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
             S part = A::zero();
             for (int tq = lane; 2 * tq <= No; tq += 32) part = A::fma(gser[tq], oser[No - 2 * tq], part);
             part = warp_sum(part);
-            if (lane == 0) {
-              const double pre = ((I.N / 2 - ksum) & 1) ? -bin : bin;
-              const c64 f = A::to_c64(part);
-              neumaier(s_re, k_re, pre * f.re);
-              neumaier(s_im, k_im, pre * f.im);
-            }
+            if (lane == 0) accum((I.N / 2 - ksum) & 1, false, part, 1.0);
           } else {
             // batch: lane o handles output N_det = o
             const bool odd = kind == KIND_BATCH_ODD;
@@ -797,7 +839,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
                 S q;
                 if (l == 0) q = A::zero();
                 else if (l == 1) q = A::from_c64(I.oddloop0);
-                else if ((l & 1) == 0) q = (l / 2 <= T) ? A::scale(lam[l / 2], 0.5) : A::zero();
+                else if ((l & 1) == 0) q = (l / 2 <= T) ? half_of<S>(lam[l / 2]) : A::zero();
                 else q = ((l - 1) / 2 <= T) ? mu0[(l - 1) / 2] : A::zero();
                 qv[l] = q;
               }
@@ -806,12 +848,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
               S part = A::zero();
               for (int tq = lane; 2 * tq <= Nf; tq += 32) part = A::fma(gser[tq], mu0[Nf - 2 * tq], part);
               part = warp_sum(part);
-              if (lane == 0) {
-                const double pre = ((Nf / 2 - ksum) & 1) ? -bin : bin;
-                const c64 f = A::to_c64(part);
-                neumaier(s_re, k_re, pre * f.re);
-                neumaier(s_im, k_im, pre * f.im);
-              }
+              if (lane == 0) accum((Nf / 2 - ksum) & 1, false, part, 1.0);
             }
             __syncwarp();
             for (int o = 0; o < nout; ++o) {
@@ -826,21 +863,18 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
                 for (int tq = lane; 2 * tq <= Nn; tq += 32) part = A::fma(gser[tq], oser[Nn - 2 * tq], part);
               }
               part = warp_sum(part);
-              if (lane == o % 32) {
-                const int bi = odd ? (o - 1) / 2 : o / 2;
-                double pre = c_binom[bi][g0] * bin;
-                if ((Nn / 2 - ksum) & 1) pre = -pre;
-                const c64 f = A::to_c64(part);
-                neumaier(s_re, k_re, pre * f.re);
-                neumaier(s_im, k_im, pre * f.im);
-              }
+              if (lane == o % 32) accum((Nn / 2 - ksum) & 1, false, part, c_binom[odd ? (o - 1) / 2 : o / 2][g0]);
             }
           }
         }
       }
       __syncwarp();
     }
-    if (lane < nout) P.partials[ch.part + lane] = make_double2(s_re + k_re, s_im + k_im);
+    if constexpr (A::modular) {
+      if (lane < nout) P.partials[ch.part + lane] = make_double2((double)A::to_c64(macc).re, 0.0);
+    } else {
+      if (lane < nout) P.partials[ch.part + lane] = make_double2(s_re + k_re, s_im + k_im);
+    }
     __syncwarp();
   }
 }
@@ -860,7 +894,7 @@ __device__ __forceinline__ void two_sum_merge(double& s, double& c, double s2, d
 // counters for the next execution.
 static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst, const double2* __restrict__ partials,
                               const double* __restrict__ scales, double2* __restrict__ out, unsigned int* counters,
-                              int ncounters, int total_out) {
+                              int ncounters, int total_out, unsigned int modp) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (gw < total_out) {
@@ -896,7 +930,12 @@ static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst
     }
     if (lane == 0) {
       const double sc = scales[I.scale_base + o];
-      out[gw] = make_double2((sr + cr) * sc, (si + ci) * sc);
+      if (modp) {  // residues (< 2^31) summed exactly in FP64 (fewer than 2^22 chunks), then mod p
+        const unsigned long long r = (unsigned long long)(sr + cr) % modp;
+        out[gw] = make_double2((double)(r * (unsigned long long)sc % modp), 0.0);
+      } else {
+        out[gw] = make_double2((sr + cr) * sc, (si + ci) * sc);
+      }
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0)

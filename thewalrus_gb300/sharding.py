@@ -24,7 +24,10 @@ def shard_range(steps, rank, world):
 
 
 def run_shard(instances, rank, world, precision=None):
-    """This shard's share of every instance's outputs (concatenated like ``nat.run``)."""
+    """This shard's share of every instance's outputs (concatenated like ``nat.run``).  FP64 or
+    double-float: a shard's share of an exact (modular) sieve is a residue, not an integer."""
+    if precision not in (None, "fp64", "df"):
+        raise ValueError("sharded sieves run in fp64 or df precision")
     parts, where, out = [], [], []
     for inst in instances:
         b, e = shard_range(inst.terms(), rank, world)
