@@ -82,23 +82,26 @@ def test_brute_force_small():
         assert rel(tw.hafnian(A, loop=True), oracle.brute_hafnian(A, loop=True)) < RTOL
 
 
+@pytest.mark.parametrize("precision", [None, "fp64"])  # None: the exact sieve for integer inputs
 @pytest.mark.parametrize("n", [6, 8, 12])
-def test_known_answers(n):
+def test_known_answers(n, precision):
     J = np.ones((2 * n, 2 * n))
-    assert tw.hafnian(J).real == math.factorial(2 * n) // (math.factorial(n) * 2**n)
+    assert tw.hafnian(J, precision=precision).real == math.factorial(2 * n) // (math.factorial(n) * 2**n)
     O, B = np.zeros((n, n)), np.ones((n, n))
-    assert round(tw.hafnian(np.block([[O, B], [B, O]])).real) == math.factorial(n)
+    assert round(tw.hafnian(np.block([[O, B], [B, O]]), precision=precision).real) == math.factorial(n)
     if n <= 10:
-        assert tw.hafnian(np.ones((n, n)), loop=True).real == pytest.approx(T[n], rel=1e-13)
-        assert tw.hafnian(np.ones((n + 1, n + 1)), loop=True).real == pytest.approx(T[n + 1], rel=1e-13)
-    assert tw.hafnian(np.identity(2 * n)) == 0
-    assert abs(tw.hafnian(np.identity(2 * n), loop=True) - 1) < 1e-12
-    assert tw.hafnian_repeated(np.array([[1.0]]), [2 * n]).real == pytest.approx(
+        assert tw.hafnian(np.ones((n, n)), loop=True, precision=precision).real == pytest.approx(T[n], rel=1e-13)
+        assert tw.hafnian(np.ones((n + 1, n + 1)), loop=True,
+                          precision=precision).real == pytest.approx(T[n + 1], rel=1e-13)
+    assert tw.hafnian(np.identity(2 * n), precision=precision) == 0
+    assert abs(tw.hafnian(np.identity(2 * n), loop=True, precision=precision) - 1) < 1e-12
+    assert tw.hafnian_repeated(np.array([[1.0]]), [2 * n], precision=precision).real == pytest.approx(
         math.factorial(2 * n) / (math.factorial(n) * 2**n), rel=1e-13)
 
 
-def test_all_ones_24_exact():
-    got = tw.hafnian(np.ones((24, 24)))
+@pytest.mark.parametrize("precision", [None, "fp64"])
+def test_all_ones_24_exact(precision):
+    got = tw.hafnian(np.ones((24, 24)), precision=precision)
     assert got.real == 316234143225.0 and got.imag == 0.0
 
 
@@ -110,8 +113,9 @@ def test_vs_quad_oracle(n, kind):
     ref = oracle.hafnian(A, precision="quad")
     assert rel(tw.hafnian(A), ref) < RTOL
     if kind == "adj":  # integer hafnian below 2^53: must round to the exact count
-        got = tw.hafnian(A)
+        got = tw.hafnian(A, precision="fp64")
         assert round(got.real) == round(ref.real) and abs(got.real - round(ref.real)) < 1e-6
+        assert tw.hafnian(A) == float(round(ref.real))  # default for integers: exact
 
 
 def test_loop_odd_and_repeated_vs_quad():
@@ -156,7 +160,7 @@ def test_exact_integer_graphs():
         for seed in seeds:
             A = wl.adjacency01(n, seed=seed)
             exact = oracle.exact_hafnian(A)
-            got = tw.hafnian(A)
+            got = tw.hafnian(A, precision="fp64")  # integer inputs default to the exact sieve
             assert abs(complex(got) - exact) <= 1e-12 * exact, (n, seed, got, exact)
             if exact < 2 ** 36:
                 assert round(got.real) == exact and abs(got.imag) < 0.5, (n, seed, got, exact)
@@ -168,5 +172,6 @@ def test_all_ones_exact_to_n28():
     for n in (20, 24, 26, 28):
         want = math.prod(range(n - 1, 0, -2))
         for dt in (np.float64, np.complex128):
-            got = tw.hafnian(np.ones((n, n), dtype=dt))
+            got = tw.hafnian(np.ones((n, n), dtype=dt), precision="fp64")
             assert round(got.real) == want and abs(got.imag) < 0.5, (n, dt, got, want)
+            assert tw.hafnian(np.ones((n, n), dtype=dt)) == float(want)  # default: exact for integers
