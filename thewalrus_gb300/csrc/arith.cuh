@@ -3,7 +3,7 @@
 // Five scalar types share one interface (struct Ar<S>):
 //   double  real FP64                 c64  complex FP64
 //   dfr     real double-float (FP32)  cdf  complex double-float
-//   modp<P> residues modulo a 31-bit prime P (exact integer sieves; integer pipe only)
+//   modp<P> residues modulo a 31-bit prime P in Montgomery form (exact integer sieves)
 // A double-float value is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), giving
 // a 48-bit significand from FP32 instructions only.  Products use the FMA error-free
 // transformation (err = fma(a, b, -a*b)); sums use Knuth's two-sum.  Conversions to and from
@@ -296,40 +296,61 @@ struct Ar<cdf> {
 // ---------------------------------------------------------------- residues modulo a prime
 // Exact arithmetic for integer inputs: every step of the sieve (elimination with any nonzero
 // pivot, La Budde, the series, the prefactors) is a field operation, so the sieve of an integer
-// matrix is exact in F_P; the host combines three primes by the Chinese remainder theorem.
-// Products of two residues fit 62 bits and are reduced by the compile-time constant P.
+// matrix is exact in F_P; the host combines several primes by the Chinese remainder theorem.
+// Residues are held in Montgomery form x R mod P (R = 2^32): a product is one 32x32->64
+// multiply and a Montgomery reduction (two more multiplies, a shift and a conditional
+// subtraction), all on the integer pipe.
 template <uint32_t P>
 struct modp {
-  uint32_t v;
+  uint32_t v;  // Montgomery form
+};
+
+template <uint32_t P>
+struct Montgomery {
+  // -P^-1 mod 2^32 by Newton's iteration x <- x (2 - P x), correct to 2^32 after five steps
+  static constexpr uint32_t inv_neg() {
+    uint32_t x = P;  // P x = 1 mod 2^3 for odd P
+    for (int i = 0; i < 5; ++i) x *= 2u - P * x;
+    return 0u - x;
+  }
+  static constexpr uint32_t NEG_INV = inv_neg();
+  static constexpr uint32_t R1 = (uint32_t)((1ull << 32) % P);                       // R mod P
+  static constexpr uint32_t R2 = (uint32_t)((unsigned __int128)R1 * R1 % P);          // R^2 mod P
+  __host__ __device__ static constexpr uint32_t redc(uint64_t t) {                   // t R^-1 mod P
+    const uint32_t m = (uint32_t)t * NEG_INV;
+    const uint32_t u = (uint32_t)((t + (uint64_t)m * P) >> 32);
+    return u >= P ? u - P : u;
+  }
+  __host__ __device__ static constexpr uint32_t to_mont(uint32_t x) { return redc((uint64_t)x * R2); }
 };
 
 template <uint32_t P>
 struct Ar<modp<P>> {
   using S = modp<P>;
   using Comp = modp<P>;
+  using M = Montgomery<P>;
   static constexpr int NC = 1;
   static constexpr bool cplx = false;
   static constexpr bool fp64 = true;  // exact zero tests, normalised (unit-subdiagonal) elimination
   static constexpr bool modular = true;
-  __device__ static __forceinline__ S mk(uint64_t x) { return S{(uint32_t)(x % P)}; }
   __device__ static __forceinline__ S zero() { return S{0u}; }
-  __device__ static __forceinline__ S one() { return S{1u}; }
+  __device__ static __forceinline__ S one() { return S{M::R1}; }
   __device__ static __forceinline__ S add(S a, S b) {
     const uint32_t s = a.v + b.v;  // < 2^32
     return S{s >= P ? s - P : s};
   }
   __device__ static __forceinline__ S sub(S a, S b) { return S{a.v >= b.v ? a.v - b.v : a.v + P - b.v}; }
   __device__ static __forceinline__ S neg(S a) { return S{a.v ? P - a.v : 0u}; }
-  __device__ static __forceinline__ S mul(S a, S b) { return mk((uint64_t)a.v * b.v); }
-  __device__ static __forceinline__ S fma(S a, S b, S c) { return mk((uint64_t)a.v * b.v + c.v); }
-  __device__ static __forceinline__ S fnma(S a, S b, S c) { return mk((uint64_t)a.v * (P - b.v) + c.v); }
+  __device__ static __forceinline__ S mul(S a, S b) { return S{M::redc((uint64_t)a.v * b.v)}; }
+  __device__ static __forceinline__ S fma(S a, S b, S c) { return add(mul(a, b), c); }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) { return sub(c, mul(a, b)); }
   __device__ static __forceinline__ S conj(S a) { return a; }
-  // exact for the integers and half-integers the kernel scales by
   __device__ static __forceinline__ S of_int(long long k) {
     const long long r = k % (long long)P;
-    return S{(uint32_t)(r < 0 ? r + P : r)};
+    return S{M::to_mont((uint32_t)(r < 0 ? r + P : r))};
   }
-  __device__ static __forceinline__ S half() { return S{(P + 1) / 2}; }
+  __device__ static __forceinline__ S half() { return S{M::to_mont((P + 1) / 2)}; }
+  // exact for the integers and half-integers the kernel scales by
   __device__ static __forceinline__ S scale(S a, double s) {
     const long long t = __double2ll_rn(2.0 * s);
     return mul(mul(a, of_int(t)), half());
@@ -345,9 +366,9 @@ struct Ar<modp<P>> {
   }
   __device__ static __forceinline__ S recip(S a) { return pow(a, P - 2); }  // Fermat
   __device__ static __forceinline__ S inv_int(int k) { return recip(of_int(k)); }
-  // residues travel through FP64 slots exactly (< 2^31)
+  // plain residues (< 2^31) travel through FP64 slots exactly
   __device__ static __forceinline__ S from_c64(c64 z) { return of_int(__double2ll_rn(z.re)); }
-  __device__ static __forceinline__ c64 to_c64(S a) { return {(double)a.v, 0.0}; }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {(double)M::redc(a.v), 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return a.v; }  // any nonzero pivot
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long) { return 0ull; }
   __device__ static __forceinline__ bool is_zero(S a) { return a.v == 0u; }

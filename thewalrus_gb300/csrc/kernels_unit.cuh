@@ -61,6 +61,7 @@ cudaError_t WG_CAT(sieve_tables_, WG_UNIT_NAME)(const double* binom, const doubl
   invmod[1] = 1;
   const uint64_t P = WG_UNIT_PRIME;
   for (uint64_t k = 2; k < 256; ++k) invmod[k] = (uint32_t)((P - (P / k) * invmod[P % k] % P) % P);
+  for (int k = 0; k < 256; ++k) invmod[k] = Montgomery<WG_UNIT_PRIME>::to_mont(invmod[k]);
   e = cudaMemcpyToSymbol(c_invmod, invmod, sizeof(invmod));
 #endif
   return e;

@@ -169,10 +169,11 @@ namespace wg {
 
 
 static inline void put_scalar(unsigned char* dst, int st, double re, double im) {
-  if (stype_mod(st)) {  // residue of an integer below 2^31 in magnitude (checked in prepare)
+  if (stype_mod(st)) {  // integer below 2^31 in magnitude (checked in prepare), Montgomery form
     const long long p = (long long)MOD_PRIMES[st - ST_MOD0];
     long long r = (long long)re % p;
-    const uint32_t v = (uint32_t)(r < 0 ? r + p : r);
+    const uint64_t x = (uint64_t)(r < 0 ? r + p : r);
+    const uint32_t v = (uint32_t)((x << 32) % (uint64_t)p);
     memcpy(dst, &v, 4);
     return;
   }
