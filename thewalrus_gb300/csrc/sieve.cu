@@ -625,33 +625,40 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     }
     G.wpc = wpc;
     const long long resident = (long long)g_num_sms * per_sm * wpc;
-    // chunking: about 4 chunks per resident warp (scaled), largest instances first, and no chunk
-    // above ~1000 term-equivalents of a 40-row tile (a fraction of a second of one warp), so the
-    // tail of a long batch stays short
-    constexpr double kMaxChunkCost = 6.4e7;
-    const double target =
-        std::max(1.0, std::min(total_cost / (double)(resident * 4.0 * chunk_scale), kMaxChunkCost * chunk_scale));
+    // chunking by guided self-scheduling, largest instances first: a chunk is 1/(2 chunk_scale) of
+    // a resident warp's share of the group's remaining work, capped at ~1000 term-equivalents of a
+    // 40-row tile and floored at ~4 (less for small groups).  Chunk sizes fall geometrically, so
+    // the last chunks -- the ones that decide when the launch ends -- are short: n = 40 takes
+    // 276 ms instead of 302 ms with fixed chunks of a quarter of a warp's share.
+    constexpr double kMaxChunkCost = 6.4e7, kMinChunkCost = 2.6e5;
+    const double div = 2.0 * chunk_scale * (double)resident;
+    const double min_cost = std::min(kMinChunkCost, total_cost / (4.0 * div));  // small groups: finer
+    double remaining = total_cost;
     std::stable_sort(members.begin(), members.end(), [&](int a, int b) {
       return P[a].term_cost * (double)(P[a].t_hi - P[a].t_lo) > P[b].term_cost * (double)(P[b].t_hi - P[b].t_lo);
     });
     G.chunk_begin = (int)pl->chunks.size();
     for (int i : members) {
       InstDev& d = P[i].d;
-      const long long lo = P[i].t_lo, range = P[i].t_hi - P[i].t_lo;
-      long long per = (long long)std::max(1.0, std::floor(target / P[i].term_cost));
-      if (per > range) per = range;
-      const long long nch = range > 0 ? (range + per - 1) / per : 0;
+      const double tc = P[i].term_cost;
+      const long long hi = P[i].t_hi, pmin = std::max(1LL, (long long)std::ceil(min_cost / tc));
       d.part_base = nparts;
-      d.nchunks = (int)nch;
-      for (long long c = 0; c < nch; ++c) {
+      int nch = 0;
+      for (long long t = P[i].t_lo; t < hi; ++nch) {
+        const double want = std::min(remaining / div, kMaxChunkCost * chunk_scale);
+        long long per = std::max(pmin, (long long)std::floor(want / tc));
+        per = std::min(per, hi - t);
         ChunkDev ch;
         ch.inst = i;
-        ch.part = nparts + (int)c * d.nout;
-        ch.t0 = lo + range * c / nch;
-        ch.t1 = lo + range * (c + 1) / nch;
+        ch.part = nparts + nch * d.nout;
+        ch.t0 = t;
+        ch.t1 = t + per;
         pl->chunks.push_back(ch);
+        remaining -= (double)per * tc;
+        t += per;
       }
-      nparts += (int)nch * d.nout;
+      d.nchunks = nch;
+      nparts += nch * d.nout;
     }
     G.chunk_count = (int)pl->chunks.size() - G.chunk_begin;
     G.ctas = (int)std::min<long long>((long long)g_num_sms * per_sm, (G.chunk_count + wpc - 1) / wpc);
