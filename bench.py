@@ -38,10 +38,10 @@ UNIT = "hafnians/s"
 PUBLISHED_N40_SECONDS = 41.32
 
 
-def workload(n=N_MATRIX):
+def workload(n=N_MATRIX, matrix="complex"):
     from thewalrus_gb300 import workloads as wl
 
-    return wl.complex_symmetric(n, seed=0)
+    return wl.complex_symmetric(n, seed=0) if matrix == "complex" else wl.real_signed(n, seed=0)
 
 
 def dist_env():
@@ -175,7 +175,7 @@ def run_gpu(args, rank, world, local):
 
     nat.check(nat.load().wg_init(local))
     n = args.n
-    A = workload(n)
+    A = workload(n, args.matrix)
     inst = tw.prepare_hafnian(A)
     plan = nat.Plan([inst], precision=args.precision)
     stream = torch.cuda.current_stream()
@@ -226,7 +226,7 @@ def run_gpu(args, rank, world, local):
     e2e_value = world * args.steps / e2e_s
     h2d, d2h = plan.transfer_bytes()
 
-    flops = costmodel.plain_hafnian_flops(n, complex_input=True)
+    flops = costmodel.plain_hafnian_flops(n, complex_input=args.matrix == "complex")
     mean_s = total_ms / args.steps * 1e-3
     achieved = flops / mean_s / 1e12
     peak = fp64_peak if args.precision == "fp64" else fp32_peak
@@ -245,8 +245,9 @@ def run_gpu(args, rank, world, local):
         "scaling": "weak", "vs_baseline": (value * PUBLISHED_N40_SECONDS if n == N_MATRIX else None),
         "dtype": "f64" if args.precision == "fp64" else "df32",
         "data": "synthetic",
-        "config": {"workload": "hafnian %dx%d complex128 (G+G^T)/2, seed 0, %d sieve terms"
-                               % (n, n, 2 ** (n // 2 - 1)),
+        "config": {"workload": "hafnian %dx%d %s, seed 0, %d sieve terms"
+                               % (n, n, "complex128 (G+G^T)/2" if args.matrix == "complex"
+                                  else "float64 (G+G^T)/2, G ~ N(0,1)", 2 ** (n // 2 - 1)),
                    "precision": args.precision, "parallelism": "shard-per-gpu" if world > 1 else "1 gpu",
                    "l2": "flushed between steps (256 MiB write, outside the timed events)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -560,6 +561,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--precision", choices=["fp64", "df"], default="fp64")
+    ap.add_argument("--matrix", choices=["complex", "real"], default="complex",
+                    help="the n-x-n workload: complex symmetric (the benchmark) or real signed")
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
