@@ -25,12 +25,20 @@
 namespace wg {
 
 static thread_local std::string g_err;
+// Per-device state: the selected device, and for every device the SM count and the La Budde
+// schedule tables in its memory (the constant tables live in each device's copy of the module).
 static int g_device = -1;
-static int g_num_sms = 0;
-static LbLane* g_lb_lane = nullptr;
-static LbOwner* g_lb_own = nullptr;
-static LbLane2* g_lb_lane2 = nullptr;
-static LbOwner2* g_lb_own2 = nullptr;
+static int g_num_sms = 0;  // of g_device
+constexpr int kMaxDev = 64;
+struct DevTables {
+  bool ready = false;
+  int sms = 0;
+  LbLane* lane = nullptr;
+  LbOwner* own = nullptr;
+  LbLane2* lane2 = nullptr;
+  LbOwner2* own2 = nullptr;
+};
+static DevTables g_dev[kMaxDev];
 
 static std::mutex g_init_mu;
 
@@ -64,9 +72,15 @@ static int ensure_init(int device) {
   int count = 0;
   CK(cudaGetDeviceCount(&count));
   if (count <= 0) return fail(WG_ECUDA, "no CUDA device");
-  if (dev >= count) return fail(WG_EINVAL, "device %d not present (%d devices)", dev, count);
+  if (dev >= count || dev >= kMaxDev) return fail(WG_EINVAL, "device %d not present (%d devices)", dev, count);
   CK(cudaSetDevice(dev));
-  CK(cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev));
+  DevTables& T = g_dev[dev];
+  if (T.ready) {
+    g_device = dev;
+    g_num_sms = T.sms;
+    return WG_OK;
+  }
+  CK(cudaDeviceGetAttribute(&T.sms, cudaDevAttrMultiProcessorCount, dev));
   // constant tables: binomials and reciprocals
   static double binom[BINOM_N][BINOM_N];
   for (int i = 0; i < BINOM_N; ++i)
@@ -86,22 +100,20 @@ static int ensure_init(int device) {
   for (int k = 0; k <= LB_KMAX; ++k)
     if (!lb_schedule(k, &lanes[k * 32], &own[k * (LB_KMAX + 1)]))
       return fail(WG_EINVAL, "no La Budde schedule for %d coefficients", k);
-  if (!g_lb_lane) {
-    CK(cudaMalloc(&g_lb_lane, sizeof(LbLane) * lanes.size()));
-    CK(cudaMalloc(&g_lb_own, sizeof(LbOwner) * own.size()));
-  }
-  CK(cudaMemcpy(g_lb_lane, lanes.data(), sizeof(LbLane) * lanes.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(g_lb_own, own.data(), sizeof(LbOwner) * own.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&T.lane, sizeof(LbLane) * lanes.size()));
+  CK(cudaMalloc(&T.own, sizeof(LbOwner) * own.size()));
+  CK(cudaMemcpy(T.lane, lanes.data(), sizeof(LbLane) * lanes.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(T.own, own.data(), sizeof(LbOwner) * own.size(), cudaMemcpyHostToDevice));
   std::vector<LbLane2> lanes2(LB2_IDS * 32);
   std::vector<LbOwner2> own2(LB2_IDS * (LB2_KMAX + 1));
   if (!lb_schedule2_all(lanes2.data(), own2.data())) return fail(WG_EINVAL, "no two-row La Budde schedule");
-  if (!g_lb_lane2) {
-    CK(cudaMalloc(&g_lb_lane2, sizeof(LbLane2) * lanes2.size()));
-    CK(cudaMalloc(&g_lb_own2, sizeof(LbOwner2) * own2.size()));
-  }
-  CK(cudaMemcpy(g_lb_lane2, lanes2.data(), sizeof(LbLane2) * lanes2.size(), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(g_lb_own2, own2.data(), sizeof(LbOwner2) * own2.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&T.lane2, sizeof(LbLane2) * lanes2.size()));
+  CK(cudaMalloc(&T.own2, sizeof(LbOwner2) * own2.size()));
+  CK(cudaMemcpy(T.lane2, lanes2.data(), sizeof(LbLane2) * lanes2.size(), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(T.own2, own2.data(), sizeof(LbOwner2) * own2.size(), cudaMemcpyHostToDevice));
+  T.ready = true;
   g_device = dev;
+  g_num_sms = T.sms;
   return WG_OK;
 }
 
@@ -154,6 +166,7 @@ struct wg_plan {
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> side_done;
   cudaEvent_t fork = nullptr;
+  int device = 0;  // the device the plan's memory and tables live on
 };
 
 struct wg_state {
@@ -556,6 +569,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
   const int wpc_cap = opt.max_warps_per_cta > 0 ? std::min(opt.max_warps_per_cta, 8) : 8;
   pl->use_graph = opt.use_graph != 0;
   pl->precision = precision;
+  pl->device = g_device;
   // outputs and scales in instance order
   int out = 0;
   std::vector<double> scales;
@@ -760,10 +774,11 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
   for (size_t g = 0; g < ng; ++g) {
     const Group& G = pl->groups[g];
     SieveParams p;
-    p.lb_lane = g_lb_lane;
-    p.lb_own = g_lb_own;
-    p.lb_lane2 = g_lb_lane2;
-    p.lb_own2 = g_lb_own2;
+    const DevTables& T = g_dev[pl->device];
+    p.lb_lane = T.lane;
+    p.lb_own = T.own;
+    p.lb_lane2 = T.lane2;
+    p.lb_own2 = T.own2;
     p.inst = pl->d_inst;
     p.chunks = pl->d_chunks + G.chunk_begin;
     p.nchunks = G.chunk_count;
