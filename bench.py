@@ -337,8 +337,8 @@ def run_batch(args):
     insts = [tw.prepare_hafnian(A) for A in mats] + \
         [tw.prepare_loop_hafnian_batch(B, D, list(f), c) for B, D, f, c in calls]
     sub = insts[::16]
-    cands = [{"chunk_scale": cs, "max_warps_per_cta": 0, "merge_classes": mc}
-             for cs in (0.5, 1.0, 2.0, 4.0) for mc in (False, True)]
+    cands = [{"chunk_scale": cs, "max_warps_per_cta": 0, "merge_classes": mc, "serial_groups": sg}
+             for cs in (1.0, 2.0, 4.0) for mc in (False, True) for sg in (False, True)]
     best, table = autotune.tune(sub, precision=args.precision, candidates=cands, repeats=1, use_cache=False)
     plan = nat.Plan(insts, precision=args.precision, use_graph=True, **best)
     s = torch.cuda.current_stream()

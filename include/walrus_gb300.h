@@ -131,7 +131,8 @@ typedef struct wg_plan_options {
   int32_t max_warps_per_cta;
   int32_t merge_classes;
   int32_t use_graph;
-  int32_t reserved;
+  int32_t serial_groups; /* 1: launch the groups one after another on the caller's stream (default:
+                            groups after the first on side streams, overlapping their tails) */
   void* stream;
 } wg_plan_options;
 int wg_plan_create_ex(const wg_instance* inst, int count, int precision, const wg_plan_options* options,

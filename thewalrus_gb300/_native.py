@@ -264,7 +264,7 @@ class WgPlanOptions(ctypes.Structure):
         ("max_warps_per_cta", ctypes.c_int32),
         ("merge_classes", ctypes.c_int32),
         ("use_graph", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("serial_groups", ctypes.c_int32),
         ("stream", ctypes.c_void_p),
     ]
 
@@ -277,7 +277,7 @@ class Plan:
     """
 
     def __init__(self, instances, precision="fp64", chunk_scale=1.0, max_warps_per_cta=0,
-                 merge_classes=False, use_graph=False):
+                 merge_classes=False, use_graph=False, serial_groups=False):
         self.lib = load()
         self.instances = list(instances)
         arr = (WgInstance * max(len(self.instances), 1))()
@@ -285,7 +285,7 @@ class Plan:
             arr[i] = inst.struct
         self._arr = arr
         opt = WgPlanOptions(float(chunk_scale), int(max_warps_per_cta), int(bool(merge_classes)),
-                            int(bool(use_graph)), 0, None)
+                            int(bool(use_graph)), int(bool(serial_groups)), None)
         h = ctypes.c_void_p()
         check(self.lib.wg_plan_create_ex(arr, len(self.instances), PRECISIONS[precision],
                                          ctypes.byref(opt), ctypes.byref(h)))

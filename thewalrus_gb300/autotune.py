@@ -19,10 +19,11 @@ from . import _native as nat
 __all__ = ["tune", "signature", "DEFAULT_CANDIDATES", "cached_options"]
 
 DEFAULT_CANDIDATES = [
-    {"chunk_scale": cs, "max_warps_per_cta": w, "merge_classes": mc}
+    {"chunk_scale": cs, "max_warps_per_cta": w, "merge_classes": mc, "serial_groups": sg}
     for cs in (0.5, 1.0, 2.0, 4.0)
     for w in (0, 4)
     for mc in (False, True)
+    for sg in (False, True)
 ]
 CACHE = os.path.join(nat.BUILD, "autotune.json")
 

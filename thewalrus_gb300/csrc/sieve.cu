@@ -167,6 +167,7 @@ struct wg_plan {
   std::vector<cudaEvent_t> side_done;
   cudaEvent_t fork = nullptr;
   int device = 0;  // the device the plan's memory and tables live on
+  bool serial_groups = false;
 };
 
 struct wg_state {
@@ -568,6 +569,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
   const double chunk_scale = opt.chunk_scale > 0 ? opt.chunk_scale : 1.0;
   const int wpc_cap = opt.max_warps_per_cta > 0 ? std::min(opt.max_warps_per_cta, 8) : 8;
   pl->use_graph = opt.use_graph != 0;
+  pl->serial_groups = opt.serial_groups != 0;
   pl->precision = precision;
   pl->device = g_device;
   // outputs and scales in instance order
@@ -756,7 +758,8 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
 
 static int launch_plan(wg_plan* pl, cudaStream_t st) {
   const size_t ng = pl->groups.size();
-  if (ng > 1) {
+  const bool side = ng > 1 && !pl->serial_groups;
+  if (side) {
     if (pl->side.size() < ng - 1) {
       if (!pl->fork) CK(cudaEventCreateWithFlags(&pl->fork, cudaEventDisableTiming));
       while (pl->side.size() < ng - 1) {
@@ -787,10 +790,10 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
     p.counter = pl->d_counters + g;
     p.err = pl->d_err;
     p.L = G.L;
-    const cudaStream_t gs = g == 0 ? st : pl->side[g - 1];
+    const cudaStream_t gs = (g == 0 || !side) ? st : pl->side[g - 1];
     const cudaError_t e = sieve_launch(G.stype, G.ns, p, G.ctas, G.wpc, gs);
     if (e != cudaSuccess) return fail(WG_ECUDA, "sieve launch: %s", cudaGetErrorString(e));
-    if (g > 0) {
+    if (g > 0 && side) {
       CK(cudaEventRecord(pl->side_done[g - 1], gs));
       CK(cudaStreamWaitEvent(st, pl->side_done[g - 1], 0));
     }

@@ -6,13 +6,16 @@
 //   1. gathers the term matrix AX_S (rows/cols of nonzero delta, columns scaled by delta, halves
 //      swapped) into the warp's shared-memory tile; loop variants border it with D_S / XD_S and
 //      append the odd-mode rows, so that the Krylov data of the loop terms survive the reduction;
-//   2. reduces it to upper Hessenberg form by Gaussian elimination with partial pivoting, with
-//      every subdiagonal entry normalised to exactly 1 (or 0) by a diagonal similarity, so that
-//      La Budde's recurrence needs no subdiagonal products;
-//   3. runs La Budde's recurrence for the first K coefficients of det(I - eta H);
+//   2. reduces it to upper Hessenberg form by Gaussian elimination with partial pivoting (FP64
+//      and residues: every subdiagonal entry normalised to exactly 1 or 0 by a diagonal
+//      similarity, so that La Budde's recurrence needs no subdiagonal products; double-float:
+//      classic multipliers), treating columns whose candidates are rounding residues as reduced;
+//   3. runs La Budde's recurrence for the first K coefficients of det(I - eta H), two rows per
+//      balanced pass;
 //   4. forms the term's generating function: det(I - eta H)^(-1/2) (the power-trace
 //      exponential of f / f_loop), times exp of the loop terms for the loop variants;
-//   5. adds prefactor * coefficient into lane-resident Neumaier sums.
+//   5. adds prefactor * coefficient into lane-resident Neumaier sums (residue sums for the exact
+//      sieve).
 // The reference's per-term pipeline is thewalrus/_hafnian.py:443-462 (plain), :546-569 (loop),
 // thewalrus/loop_hafnian_batch.py:86-116 / :165-201 (batch), with powertrace in
 // thewalrus/charpoly.py:301-327.
