@@ -14,8 +14,10 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/walrus_gb300.h"
@@ -582,17 +584,49 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     scales.insert(scales.end(), P[i].scales.begin(), P[i].scales.end());
   }
   pl->total_out = out;
-  // groups by (stype, ns); with merge_classes one group per scalar type, at the largest class
-  struct GKey { int st, ns; };
+  // launch shape for a per-warp workspace: warps per CTA for the most resident warps per SM
+  // (shared memory and registers decide how many CTAs fit), larger CTAs on ties -- e.g. 2 CTAs x
+  // 7 warps where 1 x 8 would leave room unused.  {wpc, CTAs per SM}; wpc 0 when none fits.
+  const int max_smem = 227 * 1024;
+  std::map<std::tuple<int, int, int>, std::pair<int, int>> shape_memo;
+  auto shape = [&](int st, int ns, int bytes) -> std::pair<int, int> {
+    const auto key = std::make_tuple(st, ns, bytes);
+    const auto it = shape_memo.find(key);
+    if (it != shape_memo.end()) return it->second;
+    const int wmax = std::min(wpc_cap, max_smem / bytes);
+    std::pair<int, int> r{0, 0};
+    if (wmax >= 1) {
+      int wpc = wmax, per_sm = sieve_occupancy(st, ns, wmax, wmax * bytes);
+      for (int w = wmax - 1; w >= std::max(1, wmax / 2); --w) {
+        const int ps = sieve_occupancy(st, ns, w, w * bytes);
+        if (ps * w > per_sm * wpc) { wpc = w; per_sm = ps; }
+      }
+      r = {wpc, per_sm};
+    }
+    shape_memo[key] = r;
+    return r;
+  };
+  // groups by (stype, ns, resident warps per SM of the instance's own workspace), so that a small
+  // instance does not run at the occupancy of a larger one's workspace; with merge_classes one
+  // group per scalar type, at the largest class
+  struct GKey { int st, ns, res; };
   std::vector<GKey> keys;
   std::vector<int> gid(count);
   for (int i = 0; i < count; ++i) {
     const int ns = pick_ns(P[i].stype, P[i].rows_max);
     if (ns < 0) return fail(WG_EINVAL, "instance %d: term matrix too large", i);
+    int res = 0;
+    if (!opt.merge_classes) {
+      const WarpLayout Li = make_layout(P[i].stype, std::max(P[i].rows_max, 1), std::max(P[i].mb_max, 1),
+                                        P[i].kc_max, std::max(P[i].nser_need, 2), std::max(P[i].narr, 2),
+                                        P[i].tile_ok);
+      const auto sh = shape(P[i].stype, ns, Li.bytes);
+      res = sh.first * sh.second;
+    }
     int g = -1;
     for (size_t k = 0; k < keys.size(); ++k)
-      if (keys[k].st == P[i].stype && (opt.merge_classes || keys[k].ns == ns)) g = (int)k;
-    if (g < 0) { keys.push_back({P[i].stype, ns}); g = (int)keys.size() - 1; }
+      if (keys[k].st == P[i].stype && (opt.merge_classes || (keys[k].ns == ns && keys[k].res == res))) g = (int)k;
+    if (g < 0) { keys.push_back({P[i].stype, ns, res}); g = (int)keys.size() - 1; }
     if (keys[g].ns < ns) keys[g].ns = ns;
     gid[i] = g;
   }
@@ -625,16 +659,9 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
         total_cost += P[i].term_cost * (double)(P[i].t_hi - P[i].t_lo);
       }
     G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
-    const int max_smem = 227 * 1024;
-    const int wmax = std::min(wpc_cap, max_smem / G.L.bytes);
-    if (wmax < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
-    // warps per CTA: the most resident warps per SM (shared memory and registers decide how many
-    // CTAs fit), larger CTAs on ties -- e.g. 2 CTAs x 7 warps where 1 x 8 would leave room unused
-    int wpc = wmax, per_sm = sieve_occupancy(G.stype, G.ns, wmax, wmax * G.L.bytes);
-    for (int w = wmax - 1; w >= std::max(1, wmax / 2); --w) {
-      const int ps = sieve_occupancy(G.stype, G.ns, w, w * G.L.bytes);
-      if (ps * w > per_sm * wpc) { wpc = w; per_sm = ps; }
-    }
+    if (max_smem / G.L.bytes < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
+    const auto sh = shape(G.stype, G.ns, G.L.bytes);
+    const int wpc = sh.first, per_sm = sh.second;
     if (per_sm < 1) {
       cudaGetLastError();
       return fail(WG_ECUDA, "sieve kernel cannot be resident (workspace %d B x %d warps)", G.L.bytes, wpc);
