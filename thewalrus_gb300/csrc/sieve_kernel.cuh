@@ -188,6 +188,82 @@ __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
   s = t;
 }
 
+// Column j+1 of the elimination's similarity for rows lane + 32 k, k < NF (whole 32-row blocks):
+// W[a][j+1] = sum_{b=j+1}^{mb-1} W[a][b] x[b], one row per lane.
+template <class S, int NF>
+__device__ __forceinline__ void phase_b_rows(S* __restrict__ W, const S* __restrict__ xv, int ldw, int j, int mb) {
+  using A = Ar<S>;
+  const int lane = threadIdx.x & 31;
+  S acc[NF];
+#pragma unroll
+  for (int k = 0; k < NF; ++k) acc[k] = A::zero();
+  for (int b = j + 1; b < mb; ++b) {
+    const S xb = xv[b];
+#pragma unroll
+    for (int k = 0; k < NF; ++k) acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], xb, acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < NF; ++k) W[(lane + 32 * k) * ldw + j + 1] = acc[k];
+}
+
+// The same for rows base .. rows-1 (fewer than 32, SL = ceil((rows - base) / 8) slots of 8):
+// lane = r8 + 8 c4 sums b = j+1+c4, j+5+c4, ... for rows base + r8 + 8 s, and a reduce-scatter
+// over the four column lanes (lane bits 3 and 4) leaves each row's total with one lane.
+template <class S, int SL>
+__device__ __forceinline__ void phase_b_split(S* __restrict__ W, const S* __restrict__ xv, int ldw, int j, int mb,
+                                              int rows, int base) {
+  using A = Ar<S>;
+  using Comp = typename A::Comp;
+  const int lane = threadIdx.x & 31;
+  const int r8 = lane & 7, c4 = lane >> 3;
+  constexpr int NCOMP = SL * A::NC;
+  constexpr int NCP = (NCOMP + 3) / 4 * 4;  // padded so the slots split over the 4 column lanes
+  S acc[SL];
+#pragma unroll
+  for (int s = 0; s < SL; ++s) acc[s] = A::zero();
+  const int iters = (mb - j - 1 + 3) >> 2;  // warp-uniform trip count
+  for (int it = 0; it < iters; ++it) {
+    const int b = j + 1 + c4 + 4 * it;
+    const S xb = b < mb ? xv[b] : A::zero();
+#pragma unroll
+    for (int s = 0; s < SL; ++s) {
+      const int a = base + r8 + 8 * s;
+      if (b < mb && a < rows) acc[s] = A::fma(W[a * ldw + b], xb, acc[s]);
+    }
+  }
+  Comp v[NCP];
+#pragma unroll
+  for (int s = 0; s < SL; ++s)
+#pragma unroll
+    for (int c = 0; c < A::NC; ++c) v[s * A::NC + c] = A::comp(acc[s], c);
+#pragma unroll
+  for (int i = NCOMP; i < NCP; ++i) v[i] = A::comp(A::zero(), 0);
+  const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
+  Comp u[NCP / 2];
+#pragma unroll
+  for (int i = 0; i < NCP / 2; ++i) {
+    Comp send = h1 ? v[i] : v[NCP / 2 + i];
+    Comp keep = h1 ? v[NCP / 2 + i] : v[i];
+    u[i] = A::cadd(keep, A::shfl_xor(send, 16));
+  }
+  Comp z[NCP / 4];
+#pragma unroll
+  for (int i = 0; i < NCP / 4; ++i) {
+    Comp send = h2 ? u[i] : u[NCP / 4 + i];
+    Comp keep = h2 ? u[NCP / 4 + i] : u[i];
+    z[i] = A::cadd(keep, A::shfl_xor(send, 8));
+  }
+  __syncwarp();
+  const int off = (h1 ? NCP / 2 : 0) + (h2 ? NCP / 4 : 0);
+#pragma unroll
+  for (int i = 0; i < NCP / 4; ++i) {
+    const int vi = off + i;
+    const int s = vi / A::NC, part = vi % A::NC;
+    const int a = base + r8 + 8 * s;
+    if (vi < NCOMP && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
+  }
+}
+
 // ------------------------------------------------------------------------------------------
 // Hessenberg reduction of the warp's tile by Gaussian elimination with partial pivoting.
 // W is rows x ldw (row-major); the square part is mb x mb; rows mb..rows-1 are extra row
@@ -200,14 +276,10 @@ __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
 // this scaling, which FP64's exponent range absorbs but FP32's does not, so
 // double-float scalars use the classic form: multipliers l = W[a][j]/piv (|l| <= 1),
 // W[j+1][j] keeps the pivot and column j+1 += sum_b W[:,b] l_b.
-template <class S, int NS>
+template <class S>
 __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, int rows, int ldw, int nb) {
   using A = Ar<S>;
-  using Comp = typename A::Comp;
   const int lane = threadIdx.x & 31;
-  const int r8 = lane & 7, c4 = lane >> 3;
-  constexpr int NCOMP = NS * A::NC;
-  constexpr int NCP = (NCOMP + 3) / 4 * 4;  // padded so the slots split over the 4 column lanes
 
   for (int j = 0; j + 1 < mb; ++j) {
     // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1 (ties: lowest row).  The
@@ -298,49 +370,25 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
       }
     }
     __syncwarp();
-    // --- phase B: W[a][j+1] = sum_{b=j+1}^{mb-1} W[a][b] x[b] for every row (8 row lanes x 4 col lanes)
-    S acc[NS];
-#pragma unroll
-    for (int s = 0; s < NS; ++s) acc[s] = A::zero();
-    for (int b = j + 1 + c4; b < mb; b += 4) {
-      const S xb = xv[b];
-#pragma unroll
-      for (int s = 0; s < NS; ++s) {
-        const int a = r8 + 8 * s;
-        if (8 * s < rows && a < rows) acc[s] = A::fma(W[a * ldw + b], xb, acc[s]);
+    // --- phase B: W[a][j+1] = sum_{b=j+1}^{mb-1} W[a][b] x[b] for every row a < rows.  Whole
+    // 32-row blocks take one row per lane, summed in b order (every lane busy, no cross-lane
+    // reduction); the rows after them (fewer than 32) take 8 row lanes x 4 column lanes over just
+    // the 8-row slots they fill, then a reduce-scatter over the column lanes.  The branches are
+    // warp-uniform, so no FP64 instruction is issued for an empty slot.
+    const int nfull = rows >> 5;
+    for (int k0 = 0; k0 < nfull; k0 += 2) {
+      if (nfull - k0 >= 2) phase_b_rows<S, 2>(W + 32 * k0 * ldw, xv, ldw, j, mb);
+      else phase_b_rows<S, 1>(W + 32 * k0 * ldw, xv, ldw, j, mb);
+    }
+    const int rem = rows & 31;
+    if (rem > 0) {
+      const int base = rows - rem;
+      switch ((rem + 7) >> 3) {
+        case 1: phase_b_split<S, 1>(W, xv, ldw, j, mb, rows, base); break;
+        case 2: phase_b_split<S, 2>(W, xv, ldw, j, mb, rows, base); break;
+        case 3: phase_b_split<S, 3>(W, xv, ldw, j, mb, rows, base); break;
+        default: phase_b_split<S, 4>(W, xv, ldw, j, mb, rows, base); break;
       }
-    }
-    // reduce-scatter across the 4 column lanes (lane bits 3 and 4)
-    Comp v[NCP];
-#pragma unroll
-    for (int s = 0; s < NS; ++s)
-#pragma unroll
-      for (int c = 0; c < A::NC; ++c) v[s * A::NC + c] = A::comp(acc[s], c);
-#pragma unroll
-    for (int i = NCOMP; i < NCP; ++i) v[i] = A::comp(A::zero(), 0);
-    const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
-    Comp u[NCP / 2];
-#pragma unroll
-    for (int i = 0; i < NCP / 2; ++i) {
-      Comp send = h1 ? v[i] : v[NCP / 2 + i];
-      Comp keep = h1 ? v[NCP / 2 + i] : v[i];
-      u[i] = A::cadd(keep, A::shfl_xor(send, 16));
-    }
-    Comp z[NCP / 4];
-#pragma unroll
-    for (int i = 0; i < NCP / 4; ++i) {
-      Comp send = h2 ? u[i] : u[NCP / 4 + i];
-      Comp keep = h2 ? u[NCP / 4 + i] : u[i];
-      z[i] = A::cadd(keep, A::shfl_xor(send, 8));
-    }
-    __syncwarp();
-    const int base = (h1 ? NCP / 2 : 0) + (h2 ? NCP / 4 : 0);
-#pragma unroll
-    for (int i = 0; i < NCP / 4; ++i) {
-      const int vi = base + i;
-      const int s = vi / A::NC, part = vi % A::NC;
-      const int a = r8 + 8 * s;
-      if (vi < NCOMP && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
     }
     __syncwarp();
   }
@@ -717,6 +765,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       }
       const int delta = lane < E ? (glynn ? 2 * g - rep : g) : 0;
       const unsigned nz = __ballot_sync(0xffffffffu, delta != 0);
+      const bool unit_delta = __all_sync(0xffffffffu, delta >= -1 && delta <= 1);  // signs only
       const int Ep = __popc(nz);
       const int m = 2 * Ep;
       const int mb = m + nb;
@@ -778,16 +827,26 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
         const int total = rows * mb;
         const int dr = 32 / mb, dc = 32 % mb;
         int r = lane / mb, cc = lane % mb;
-        for (int e = lane; e < total; e += 32) {
-          const S x = Aext[(size_t)srow[r] * lda + scol[cc]];
-          W[r * ldw + cc] = scale_int(x, sdel[cc]);
-          cc += dc;
-          r += dr;
-          if (cc >= mb) { cc -= mb; r += 1; }
+        if (unit_delta) {  // sign flips on the integer pipe
+          for (int e = lane; e < total; e += 32) {
+            const S x = Aext[(size_t)srow[r] * lda + scol[cc]];
+            W[r * ldw + cc] = sdel[cc] < 0 ? A::neg(x) : x;
+            cc += dc;
+            r += dr;
+            if (cc >= mb) { cc -= mb; r += 1; }
+          }
+        } else {
+          for (int e = lane; e < total; e += 32) {
+            const S x = Aext[(size_t)srow[r] * lda + scol[cc]];
+            W[r * ldw + cc] = scale_int(x, sdel[cc]);
+            cc += dc;
+            r += dr;
+            if (cc >= mb) { cc -= mb; r += 1; }
+          }
         }
       }
       __syncwarp();
-      hessenberg_elim<S, NS>(W, xv, mb, rows, ldw, nb);
+      hessenberg_elim<S>(W, xv, mb, rows, ldw, nb);
       // loop variants: Krylov data of the border first (La Budde then reuses the tile)
       if (kind != KIND_PLAIN) loop_krylov<S>(W, ldw, m, mb, ne, I.K, xv, eser, lam, mu, mu0);
       // characteristic polynomial coefficients of the block (xv caches the subdiagonal)
