@@ -262,9 +262,10 @@ def run_gpu(args, rank, world, local):
         "result": [float(np.real(result)), float(np.imag(result))],
         "e2e_result_matches": bool(abs(r - result) <= 1e-12 * abs(result)),
     }
-    if n != N_MATRIX:
-        line["metric"] = "n=%d hafnians/s (complex128, Glynn sieve)" % n
-    if not args.no_cpu_baseline and n == N_MATRIX:
+    if n != N_MATRIX or args.matrix != "complex":
+        line["metric"] = "n=%d hafnians/s (%s, Glynn sieve)" % (
+            n, "complex128" if args.matrix == "complex" else "float64")
+    if not args.no_cpu_baseline and n == N_MATRIX and args.matrix == "complex":
         rate, info = cpu_sample(seconds=args.cpu_seconds)
         line["cpu_baseline"] = {
             "value": rate, "unit": UNIT, "cores": info["threads"], "kind": "port",
