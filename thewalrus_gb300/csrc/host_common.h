@@ -87,6 +87,9 @@ static inline cudaError_t sieve_tables_all(const double* binom, const double* in
 static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int nser, int narr, bool tilewin) {
   WarpLayout L;
   const int sb = (int)stype_bytes(stype);
+  // FP64 and modular scalars run the normalised elimination (unit subdiagonal), so La Budde reads
+  // its T_r = H(i-r, i) straight from the tile; double-float keeps the beta products in tb
+  const bool normalised = stype != ST_REALDF && stype != ST_CPLXDF;
   auto al = [](int x) { return (x + 15) & ~15; };
   L.ldw = std::max(mb, 1) | 1;
   L.rows = std::max(rows, 1);
@@ -97,15 +100,26 @@ static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int ns
   off += al(L.ldw * sb);
   L.off_win = off;
   L.tilewin = tilewin ? 1 : 0;
-  off += al((tilewin ? 3 : L.kw) * L.kw * sb);
+  // tile mode: La Budde rows 0..2 only (row i' has entries 0..i'), stride 3; otherwise a
+  // circular window of kw rows of kw entries
+  off += al((tilewin ? 9 : L.kw * L.kw) * sb);
   L.off_tb = off;
-  off += al(2 * L.kw * sb);  // T_r of two rows
-  L.off_part = off;
-  off += al(96 * sb);  // La Budde piece partials (3 per lane)
-  L.off_ser = off;
-  off += al(narr * L.nser * sb);
+  if (!normalised) off += al(2 * L.kw * sb);  // T_r of two rows
+  // La Budde piece partials (3 per lane) are dead outside La Budde; with the two series arrays of
+  // the plain kinds (written after La Budde) they share one region
+  const int part_bytes = al(96 * sb), ser_bytes = al(narr * L.nser * sb);
+  if (narr <= 2) {
+    L.off_part = off;
+    L.off_ser = off;
+    off += std::max(part_bytes, ser_bytes);
+  } else {
+    L.off_part = off;
+    off += part_bytes;
+    L.off_ser = off;
+    off += ser_bytes;
+  }
   L.off_int = off;
-  off += al((L.rows + 2 * L.ldw) * 4);
+  off += al((L.rows + 2 * L.ldw) * 2);  // 16-bit row, column and delta maps
   L.bytes = al(off);
   return L;
 }

@@ -193,7 +193,7 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   if (ns < 0) return err(WG_EINVAL, "size beyond the maximum: term matrix too large");
   bool all_odd = d.glynn != 0;
   for (int i = 0; i < E; ++i) all_odd = all_odd && (edge_reps[i] % 2 == 1);
-  const WarpLayout L = make_layout(st, m_max, m_max, std::min(d.K, m_max), std::max(d.K, m_max) + 2, 2,
+  const WarpLayout L = make_layout(st, m_max, m_max, std::min(d.K, m_max), d.K + 2, 2,
                                    all_odd && d.K < m_max);
   const int wpc = std::min(8, (227 * 1024) / L.bytes);
   if (wpc < 1) return err(WG_EINVAL, "size beyond the maximum: per-warp workspace does not fit");

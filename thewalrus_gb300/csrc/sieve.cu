@@ -359,7 +359,9 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
   P.mb_max = m_max + nb;
   P.rows_max = m_max + nb + ne;
   P.kc_max = std::min(d.K, m_max);
-  P.nser_need = std::max(std::max(d.K, d.Nodd), std::max(Nf, m_max)) + 2;
+  // plain kinds keep det coefficients and the series (K + 1 each); loop kinds also the odd
+  // series (Nodd, Nf) and the Krylov vectors (m + 1)
+  P.nser_need = kind == KIND_PLAIN ? d.K + 2 : std::max(std::max(d.K, d.Nodd), std::max(Nf, m_max)) + 2;
   P.narr = (kind == KIND_PLAIN) ? 2 : 8;
   {
     // a term with m < K+1 and no border/extra rows has columns shorter than Kc+1: only when

@@ -396,12 +396,13 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
 
 // ------------------------------------------------------------------------------------------
 // Storage of La Budde's coefficient rows c[i'][0..Kc].  Tile mode: rows 0..2 live in `win`
-// (3 x kw) and row i' >= 3 down block column i'-2 of the tile, which is dead by then (column c
-// is last read at step c+1, the subdiagonal entries being cached); otherwise a circular window of
-// kw rows (slot = i' mod kw) when the tile cannot hold Kc+1 entries per column.
+// (stride 3: row i' is only ever read at entries 0..i', its degree) and row i' >= 3 down block
+// column i'-3 of the tile, which is dead by then (column c is last read at step c+1, the
+// subdiagonal entries being cached); otherwise a circular window of kw rows (slot = i' mod kw)
+// when the tile cannot hold Kc+1 entries per column.
 template <class S>
 __device__ __forceinline__ S& cw_at(S* W, int ldw, int nb, S* win, int kw, bool tile, int ip, int slot, int u) {
-  if (tile) return ip >= 3 ? W[u * ldw + nb + ip - 3] : win[ip * kw + u];
+  if (tile) return ip >= 3 ? W[u * ldw + nb + ip - 3] : win[ip * 3 + u];
   return win[slot * kw + u];
 }
 
@@ -419,14 +420,17 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
   for (int k = lane + 2; k <= m; k += 32) bet[k] = W[(nb + k - 1) * ldw + nb + k - 2];
-  for (int jj = lane; jj <= Kc; jj += 32) cw_at(W, ldw, nb, win, kw, tile, 0, 0, jj) = (jj == 0) ? A::one() : A::zero();
+  for (int jj = lane; jj <= (tile ? 0 : Kc); jj += 32)
+    cw_at(W, ldw, nb, win, kw, tile, 0, 0, jj) = (jj == 0) ? A::one() : A::zero();
   __syncwarp();
   int zlast = 1;
   int prow = 0;  // circular-window slot of row i-1
   // subdiagonal products P(i, r) = beta_i ... beta_{i-r+1} for r = lane+1 and lane+33, kept in
   // registers across rows: P(i, r) = beta_i * P(i-1, r-1), P(i, 1) = beta_i
   S pr0 = A::zero(), pr1 = A::zero();
-  // T_r of row i into tbr[1..R]; returns the last usable r
+  // T_r of row i: the normalised forms read T_r = H(i-r, i) from tile column nb+i-1 (still
+  // intact: La Budde rows go to columns up to nb+i-3), the others get tbr[1..R] filled; returns
+  // the last usable r
   auto fill_tb = [&](int i, S* tbr) -> int {
     const int wi = nb + i - 1;
     const int R = (i - 1) < (Kc - 1) ? (i - 1) : (Kc - 1);
@@ -434,7 +438,6 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
     if constexpr (A::fp64) {
       if (i >= 2 && A::is_zero(bet[i])) zlast = i;
       rcap = (i - zlast) < R ? (i - zlast) : R;
-      for (int r = lane + 1; r <= rcap; r += 32) tbr[r] = W[(wi - r) * ldw + wi];
     } else {
       const S bi = i >= 2 ? bet[i] : A::zero();
       const S up0 = shfl_up_s(pr0, 1);  // P(i-1, r-1) for r = lane+1
@@ -480,7 +483,8 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
             int slot = prow + row - r;  // circular slot of row i+row-r-1
             if (slot < 0) slot += kw;
             const S cv = cw_at(W, ldw, nb, win, kw, tile, i + row - r - 1, slot, j - r - 1);
-            acc = A::fma(tb[row * kw + r], cv, acc);
+            const S tr = A::fp64 ? W[(wi + row - r) * ldw + wi + row] : tb[row * kw + r];
+            acc = A::fma(tr, cv, acc);
           }
         }
         if (tot > 0) part[3 * lane + (l2 > 0 ? 2 : (l1 > 0 ? 1 : 0))] = acc;
@@ -533,8 +537,9 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
           int slot = prow - r;  // circular slot of row i-r-1 (row i-1 is in prow)
           if (slot < 0) slot += kw;
           const S cv = cw_at(W, ldw, nb, win, kw, tile, i - r - 1, slot, j - r - 1);
-          if (it & 1) acc1 = A::fma(tb[r], cv, acc1);
-          else acc0 = A::fma(tb[r], cv, acc0);
+          const S tr = A::fp64 ? W[(wi - r) * ldw + wi] : tb[r];
+          if (it & 1) acc1 = A::fma(tr, cv, acc1);
+          else acc0 = A::fma(tr, cv, acc0);
         }
       }
       const S acc = A::add(acc0, acc1);
@@ -702,9 +707,9 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
   S* tb = reinterpret_cast<S*>(ws + L.off_tb);
   S* lbpart = reinterpret_cast<S*>(ws + L.off_part);
   S* ser = reinterpret_cast<S*>(ws + L.off_ser);
-  int* srow = reinterpret_cast<int*>(ws + L.off_int);
-  int* scol = srow + L.rows;
-  int* sdel = scol + L.ldw;
+  short* srow = reinterpret_cast<short*>(ws + L.off_int);
+  short* scol = srow + L.rows;
+  short* sdel = scol + L.ldw;
   const int ldw = L.ldw;
   const int ns = L.nser;
   S* cpoly = ser;           // [0, ns)
@@ -812,15 +817,15 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       // index maps of the tile
       if (delta != 0) {
         const int pos = __popc(nz & ((1u << lane) - 1u));
-        srow[nb + pos] = lane;
-        srow[nb + Ep + pos] = E + lane;
-        scol[nb + pos] = E + lane;
-        scol[nb + Ep + pos] = lane;
-        sdel[nb + pos] = delta;
-        sdel[nb + Ep + pos] = delta;
+        srow[nb + pos] = (short)lane;
+        srow[nb + Ep + pos] = (short)(E + lane);
+        scol[nb + pos] = (short)(E + lane);
+        scol[nb + Ep + pos] = (short)lane;
+        sdel[nb + pos] = (short)delta;
+        sdel[nb + Ep + pos] = (short)delta;
       }
-      if (lane == 0 && nb) { srow[0] = n; scol[0] = n; sdel[0] = 1; }
-      if (lane < ne) srow[mb + lane] = n + 1 + lane;
+      if (lane == 0 && nb) { srow[0] = (short)n; scol[0] = (short)n; sdel[0] = 1; }
+      if (lane < ne) srow[mb + lane] = (short)(n + 1 + lane);
       __syncwarp();
       // gather the tile
       if (mb > 0) {
