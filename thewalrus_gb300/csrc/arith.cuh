@@ -144,6 +144,8 @@ struct Ar<double> {
   __device__ static __forceinline__ c64 to_c64(S a) { return {a, 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a); }
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_d(k); }
+  // 32-bit pivot key: sign-free exponent and the top 20 mantissa bits
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a) == 0; }
   __device__ static __forceinline__ S recip(S a) { return recip_newton(a); }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
@@ -186,6 +188,8 @@ struct Ar<c64> {
     return x > y ? x : y;
   }
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_d(k); }
+  // 32-bit pivot key: sign-free exponent and the top 20 mantissa bits
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re) | absbits_d(a.im)) == 0; }
   __device__ static __forceinline__ S recip(S a) {
     const double d = recip_newton(::fma(a.re, a.re, a.im * a.im));
@@ -224,6 +228,7 @@ struct Ar<dfr> {
   __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a), 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_f(a.hi); }
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_f(k); }
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)k; }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_f(a.hi) == 0; }
   __device__ static __forceinline__ S recip(S a) { return df_from_d(1.0 / df_to_d(a)); }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
@@ -272,6 +277,7 @@ struct Ar<cdf> {
     return x > y ? x : y;
   }
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_f(k); }
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)k; }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_f(a.re.hi) | absbits_f(a.im.hi)) == 0; }
   __device__ static __forceinline__ S recip(S a) {
     c64 z = to_c64(a);
@@ -371,6 +377,7 @@ struct Ar<modp<P>> {
   __device__ static __forceinline__ c64 to_c64(S a) { return {(double)M::redc(a.v), 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return a.v; }  // any nonzero pivot
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long) { return 0ull; }
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return k ? 0x80u : 0u; }
   __device__ static __forceinline__ bool is_zero(S a) { return a.v == 0u; }
   __device__ static __forceinline__ Comp comp(const S& a, int) { return a; }
   __device__ static __forceinline__ void set_comp(S& a, int, Comp v) { a = v; }

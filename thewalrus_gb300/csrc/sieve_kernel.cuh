@@ -282,34 +282,32 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
   const int lane = threadIdx.x & 31;
 
   for (int j = 0; j + 1 < mb; ++j) {
-    // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1 (ties: lowest row).  The
-    // same pass takes each lane's largest key over the column's block rows nb..j (uk, never
-    // reduced): the column is deflated when some lane's uk puts the best candidate at or below
-    // the deflation threshold, i.e. when max uk does -- one vote, off the shuffle chain.
-    unsigned long long bk = 0, uk = 0;
-    int bi = j + 1;
+    // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1, to 13 (FP64) or 16 (FP32
+    // high part) significant bits, ties to the lowest row: the key's top bits and 127 - row packed
+    // into one word, so one warp max-reduction picks it.  The same pass takes each lane's largest
+    // key over the column's block rows nb..j (uk, never reduced): the column is deflated when
+    // some lane's uk puts the best candidate at or below the deflation threshold, i.e. when max
+    // uk does -- one vote, off the reduction.
+    unsigned best = 0;
+    unsigned long long uk = 0;
     for (int a = nb + lane; a < mb; a += 32) {
       const unsigned long long k = A::key(W[a * ldw + j]);
       if (a > j) {
-        if (k > bk) { bk = k; bi = a; }
+        const unsigned pk = (A::key32(k) & ~0x7fu) | (unsigned)(127 - a);
+        best = pk > best ? pk : best;
       } else {
         uk = k > uk ? k : uk;
       }
     }
-#pragma unroll
-    for (int off = 16; off; off >>= 1) {
-      unsigned long long ok = __shfl_xor_sync(0xffffffffu, bk, off);
-      int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (ok > bk || (ok == bk && oi < bi)) { bk = ok; bi = oi; }
-    }
-    if (__any_sync(0xffffffffu, bk <= A::key_deflate(uk))) {
+    best = __reduce_max_sync(0xffffffffu, best);
+    if (__any_sync(0xffffffffu, (best & ~0x7fu) <= (A::key32(A::key_deflate(uk)) & ~0x7fu))) {
       // nothing to eliminate: the candidates are zero or rounding residues of an exact
       // cancellation; the subdiagonal becomes an exact zero and the column below it is cleared
       for (int a = j + 1 + lane; a < mb; a += 32) W[a * ldw + j] = A::zero();
       __syncwarp();
       continue;
     }
-    const int p = bi;
+    const int p = 127 - (int)(best & 0x7fu);
     if (p != j + 1) {
       for (int c = j + lane; c < mb; c += 32) {
         S t = W[p * ldw + c];
@@ -469,6 +467,34 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
         const int l0 = sc.len[0], l1 = sc.len[1], l2 = sc.len[2];
         const int tot = l0 + l1 + l2;
         S acc = A::zero();
+        if (A::fp64 && tile && i >= Kc + 3 && rc0 == Kc - 1 && rc1 == Kc - 1) {
+          // steady state of the tile form: every c[i+row-r-1] read lives in the tile and no
+          // subdiagonal zero truncates the sums, so along a piece both operands step linearly --
+          // T_r = W[wi+row-r][wi+row] by -ldw, c[i+row-r-1][j-r-1] = W[j-r-1][nb+i+row-r-4] by
+          // -(ldw+1) -- and an iteration is two loads and one multiply-add
+          int oT[3], oC[3];
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const int row = (sc.rowmask >> q) & 1, jq = sc.j[q], r0 = sc.rlo[q];
+            oT[q] = (wi + row - r0) * ldw + wi + row;
+            oC[q] = (jq - r0 - 1) * ldw + nb + i + row - r0 - 4;
+          }
+          int q = 0, left = l0, pT = oT[0], pC = oC[0];
+          for (int it = 0; it < tot; ++it) {
+            if (left == 0) {  // next piece
+              part[3 * lane + q] = acc;
+              acc = A::zero();
+              ++q;
+              left = q == 1 ? l1 : l2;
+              pT = q == 1 ? oT[1] : oT[2];
+              pC = q == 1 ? oC[1] : oC[2];
+            }
+            acc = A::fma(W[pT], W[pC], acc);
+            pT -= ldw;
+            pC -= ldw + 1;
+            --left;
+          }
+        } else {
         for (int it = 0; it < tot; ++it) {
           const int q = (it >= l0) + (it >= l0 + l1);
           const int start = q == 0 ? 0 : (q == 1 ? l0 : l0 + l1);
@@ -486,6 +512,7 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
             const S tr = A::fp64 ? W[(wi + row - r) * ldw + wi + row] : tb[row * kw + r];
             acc = A::fma(tr, cv, acc);
           }
+        }
         }
         if (tot > 0) part[3 * lane + (l2 > 0 ? 2 : (l1 > 0 ? 1 : 0))] = acc;
       }
