@@ -103,8 +103,13 @@ static inline WarpLayout make_layout(int stype, int rows, int mb, int kc, int ns
   // tile mode: La Budde rows 0..2 only (row i' has entries 0..i'), stride 3; otherwise a
   // circular window of kw rows of kw entries
   off += al((tilewin ? 9 : L.kw * L.kw) * sb);
+  // double-float T_r of two rows (entries r = 1..kw-2 of rows 0 and 1): in the x row, dead during
+  // La Budde, when it is long enough
   L.off_tb = off;
-  if (!normalised) off += al(2 * L.kw * sb);  // T_r of two rows
+  if (!normalised) {
+    if (2 * L.kw - 1 <= L.ldw) L.off_tb = L.off_x;
+    else off += al(2 * L.kw * sb);
+  }
   // La Budde piece partials (3 per lane) are dead outside La Budde; with the two series arrays of
   // the plain kinds (written after La Budde) they share one region
   const int part_bytes = al(96 * sb), ser_bytes = al(narr * L.nser * sb);

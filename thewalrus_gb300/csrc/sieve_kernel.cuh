@@ -395,9 +395,9 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
 // ------------------------------------------------------------------------------------------
 // Storage of La Budde's coefficient rows c[i'][0..Kc].  Tile mode: rows 0..2 live in `win`
 // (stride 3: row i' is only ever read at entries 0..i', its degree) and row i' >= 3 down block
-// column i'-3 of the tile, which is dead by then (column c is last read at step c+1, the
-// subdiagonal entries being cached); otherwise a circular window of kw rows (slot = i' mod kw)
-// when the tile cannot hold Kc+1 entries per column.
+// column i'-3 of the tile, which is dead by then (block column c is read at step c+1 for T_r and
+// alpha and last at step c+2 for the subdiagonal entry); otherwise a circular window of kw rows
+// (slot = i' mod kw) when the tile cannot hold Kc+1 entries per column.
 template <class S>
 __device__ __forceinline__ S& cw_at(S* W, int ldw, int nb, S* win, int kw, bool tile, int ip, int slot, int u) {
   if (tile) return ip >= 3 ? W[u * ldw + nb + ip - 3] : win[ip * 3 + u];
@@ -412,12 +412,11 @@ __device__ __forceinline__ S& cw_at(S* W, int ldw, int nb, S* win, int kw, bool 
 // up to the last zero beta; otherwise the beta products come from a lane prefix-product scan.
 template <class S>
 __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __restrict__ win, int kw, bool tile,
-                        S* __restrict__ bet, S* __restrict__ tb, S* __restrict__ part, S* __restrict__ cpoly,
+                        S* __restrict__ tb, S* __restrict__ part, S* __restrict__ cpoly,
                         const LbLane* __restrict__ lbl, const LbOwner* __restrict__ lbo,
                         const LbLane2* __restrict__ lbl2, const LbOwner2* __restrict__ lbo2) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
-  for (int k = lane + 2; k <= m; k += 32) bet[k] = W[(nb + k - 1) * ldw + nb + k - 2];
   for (int jj = lane; jj <= (tile ? 0 : Kc); jj += 32)
     cw_at(W, ldw, nb, win, kw, tile, 0, 0, jj) = (jj == 0) ? A::one() : A::zero();
   __syncwarp();
@@ -434,10 +433,10 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
     const int R = (i - 1) < (Kc - 1) ? (i - 1) : (Kc - 1);
     int rcap = R;
     if constexpr (A::fp64) {
-      if (i >= 2 && A::is_zero(bet[i])) zlast = i;
+      if (i >= 2 && A::is_zero(W[wi * ldw + wi - 1])) zlast = i;
       rcap = (i - zlast) < R ? (i - zlast) : R;
     } else {
-      const S bi = i >= 2 ? bet[i] : A::zero();
+      const S bi = i >= 2 ? W[wi * ldw + wi - 1] : A::zero();
       const S up0 = shfl_up_s(pr0, 1);  // P(i-1, r-1) for r = lane+1
       const S up1 = shfl_up_s(pr1, 1);
       const S last0 = A::shfl(pr0, 31);  // P(i-1, 32) feeds r = 33
@@ -881,9 +880,9 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       hessenberg_elim<S>(W, xv, mb, rows, ldw, nb);
       // loop variants: Krylov data of the border first (La Budde then reuses the tile)
       if (kind != KIND_PLAIN) loop_krylov<S>(W, ldw, m, mb, ne, I.K, xv, eser, lam, mu, mu0);
-      // characteristic polynomial coefficients of the block (xv caches the subdiagonal)
+      // characteristic polynomial coefficients of the block (xv is free again: it may hold tb)
       const int Kc = I.K < m ? I.K : m;
-      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, L.tilewin != 0, xv, tb, lbpart, cpoly, P.lb_lane, P.lb_own,
+      labudde<S>(W, ldw, nb, m, Kc, win, L.kw, L.tilewin != 0, tb, lbpart, cpoly, P.lb_lane, P.lb_own,
                  P.lb_lane2, P.lb_own2);
       const int Gdeg = I.K;  // degree of det^(-1/2) needed
       inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
