@@ -1,6 +1,6 @@
 // Host-side helpers shared by the translation units that launch the sieve kernels:
-// scalar classes, register classes, per-warp shared-memory layout and the La Budde lane
-// schedule.
+// scalar classes, the tile size limit, per-warp shared-memory layout and the La Budde lane
+// schedules.
 #pragma once
 #include <algorithm>
 #include <vector>
@@ -11,8 +11,8 @@
 namespace wg {
 
 // kernel launch and occupancy by scalar class (the kernels live in kernels_*.cu)
-static inline cudaError_t sieve_launch(int stype, int ns, const SieveParams& p, int ctas, int wpc, cudaStream_t st);
-static inline int sieve_occupancy(int stype, int ns, int wpc, int smem);
+static inline cudaError_t sieve_launch(int stype, const SieveParams& p, int ctas, int wpc, cudaStream_t st);
+static inline int sieve_occupancy(int stype, int wpc, int smem);
 static inline cudaError_t sieve_tables_all(const double* binom, const double* inv);
 
 // scalar classes
@@ -25,48 +25,37 @@ static size_t stype_bytes(int st) {
 }
 static const uint32_t MOD_PRIMES[5] = {2147483647u, 2147483629u, 2147483587u, 2147483579u, 2147483563u};
 
-// register classes: rows of the term tile per row lane (8 row lanes).  Row slots beyond the
-// tile are skipped by a warp-uniform branch, so a class larger than needed costs registers, not
-// FP64 issue slots; a few classes keep the build small.
-static const int NS_CPLX[] = {4, 6, 8, 10};
-static const int NS_REAL[] = {4, 8, 12};
-
-static inline int pick_ns(int stype, int rows) {
-  if (stype == ST_CPLX64 || stype == ST_CPLXDF) {
-    for (int ns : NS_CPLX)
-      if (8 * ns >= rows) return ns;
-  } else {
-    for (int ns : NS_REAL)
-      if (8 * ns >= rows) return ns;
-  }
-  return -1;
+// the largest term tile a warp works on: 80 rows of complex scalars, 96 of real ones (the packed
+// pivot keys hold row indices below 128)
+static inline bool tile_rows_ok(int stype, int rows) {
+  return rows <= ((stype == ST_CPLX64 || stype == ST_CPLXDF) ? 80 : 96);
 }
 
-static inline cudaError_t sieve_launch(int stype, int ns, const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
+static inline cudaError_t sieve_launch(int stype, const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
   switch (stype) {
-    case ST_CPLX64: return sieve_launch_c64(ns, p, ctas, wpc, st);
-    case ST_CPLXDF: return sieve_launch_cdf(ns, p, ctas, wpc, st);
-    case ST_REAL64: return sieve_launch_f64(ns, p, ctas, wpc, st);
-    case ST_REALDF: return sieve_launch_fdf(ns, p, ctas, wpc, st);
-    case ST_MOD0: return sieve_launch_mod0(ns, p, ctas, wpc, st);
-    case ST_MOD1: return sieve_launch_mod1(ns, p, ctas, wpc, st);
-    case ST_MOD2: return sieve_launch_mod2(ns, p, ctas, wpc, st);
-    case ST_MOD3: return sieve_launch_mod3(ns, p, ctas, wpc, st);
-    default: return sieve_launch_mod4(ns, p, ctas, wpc, st);
+    case ST_CPLX64: return sieve_launch_c64(p, ctas, wpc, st);
+    case ST_CPLXDF: return sieve_launch_cdf(p, ctas, wpc, st);
+    case ST_REAL64: return sieve_launch_f64(p, ctas, wpc, st);
+    case ST_REALDF: return sieve_launch_fdf(p, ctas, wpc, st);
+    case ST_MOD0: return sieve_launch_mod0(p, ctas, wpc, st);
+    case ST_MOD1: return sieve_launch_mod1(p, ctas, wpc, st);
+    case ST_MOD2: return sieve_launch_mod2(p, ctas, wpc, st);
+    case ST_MOD3: return sieve_launch_mod3(p, ctas, wpc, st);
+    default: return sieve_launch_mod4(p, ctas, wpc, st);
   }
 }
 
-static inline int sieve_occupancy(int stype, int ns, int wpc, int smem) {
+static inline int sieve_occupancy(int stype, int wpc, int smem) {
   switch (stype) {
-    case ST_CPLX64: return sieve_occupancy_c64(ns, wpc, smem);
-    case ST_CPLXDF: return sieve_occupancy_cdf(ns, wpc, smem);
-    case ST_REAL64: return sieve_occupancy_f64(ns, wpc, smem);
-    case ST_REALDF: return sieve_occupancy_fdf(ns, wpc, smem);
-    case ST_MOD0: return sieve_occupancy_mod0(ns, wpc, smem);
-    case ST_MOD1: return sieve_occupancy_mod1(ns, wpc, smem);
-    case ST_MOD2: return sieve_occupancy_mod2(ns, wpc, smem);
-    case ST_MOD3: return sieve_occupancy_mod3(ns, wpc, smem);
-    default: return sieve_occupancy_mod4(ns, wpc, smem);
+    case ST_CPLX64: return sieve_occupancy_c64(wpc, smem);
+    case ST_CPLXDF: return sieve_occupancy_cdf(wpc, smem);
+    case ST_REAL64: return sieve_occupancy_f64(wpc, smem);
+    case ST_REALDF: return sieve_occupancy_fdf(wpc, smem);
+    case ST_MOD0: return sieve_occupancy_mod0(wpc, smem);
+    case ST_MOD1: return sieve_occupancy_mod1(wpc, smem);
+    case ST_MOD2: return sieve_occupancy_mod2(wpc, smem);
+    case ST_MOD3: return sieve_occupancy_mod3(wpc, smem);
+    default: return sieve_occupancy_mod4(wpc, smem);
   }
 }
 

@@ -1,14 +1,14 @@
 // Body of one kernel translation unit: define WG_UNIT_SCALAR (the scalar type), WG_UNIT_NAME (the
-// suffix of the entry points), WG_UNIT_CLASSES(X) (X(ns) for every register class) and, for the
-// residue types, WG_UNIT_PRIME, then include this file.
+// suffix of the entry points) and, for the residue types, WG_UNIT_PRIME, then include this file.
 #include "kernels.h"
 
 namespace wg {
-namespace {
 
-template <int NS>
-cudaError_t launch_ns(const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
-  auto k = sieve_kernel<WG_UNIT_SCALAR, NS>;
+#define WG_CAT2(a, b) a##b
+#define WG_CAT(a, b) WG_CAT2(a, b)
+
+cudaError_t WG_CAT(sieve_launch_, WG_UNIT_NAME)(const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
+  auto k = sieve_kernel<WG_UNIT_SCALAR>;
   const int smem = wpc * p.L.bytes;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
@@ -16,38 +16,12 @@ cudaError_t launch_ns(const SieveParams& p, int ctas, int wpc, cudaStream_t st) 
   return cudaGetLastError();
 }
 
-template <int NS>
-int occupancy_ns(int wpc, int smem) {
+int WG_CAT(sieve_occupancy_, WG_UNIT_NAME)(int wpc, int smem) {
   int nb = 0;
-  auto k = sieve_kernel<WG_UNIT_SCALAR, NS>;
+  auto k = sieve_kernel<WG_UNIT_SCALAR>;
   if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 32 * wpc, smem) != cudaSuccess) return 0;
   return nb;
-}
-
-}  // namespace
-
-#define WG_CAT2(a, b) a##b
-#define WG_CAT(a, b) WG_CAT2(a, b)
-
-cudaError_t WG_CAT(sieve_launch_, WG_UNIT_NAME)(int ns, const SieveParams& p, int ctas, int wpc, cudaStream_t st) {
-  switch (ns) {
-#define WG_CASE(NS) \
-  case NS: return launch_ns<NS>(p, ctas, wpc, st);
-    WG_UNIT_CLASSES(WG_CASE)
-#undef WG_CASE
-    default: return cudaErrorInvalidValue;
-  }
-}
-
-int WG_CAT(sieve_occupancy_, WG_UNIT_NAME)(int ns, int wpc, int smem) {
-  switch (ns) {
-#define WG_CASE(NS) \
-  case NS: return occupancy_ns<NS>(wpc, smem);
-    WG_UNIT_CLASSES(WG_CASE)
-#undef WG_CASE
-    default: return 0;
-  }
 }
 
 cudaError_t WG_CAT(sieve_tables_, WG_UNIT_NAME)(const double* binom, const double* inv) {

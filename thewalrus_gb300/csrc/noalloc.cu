@@ -189,15 +189,14 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   const int st = dtype == WG_COMPLEX128 ? ST_CPLX64 : ST_REAL64;
   const int m_max = 2 * nnz;
   if (d.K > 250) return err(WG_EINVAL, "size beyond the maximum: photon number above 250");
-  const int ns = pick_ns(st, m_max);
-  if (ns < 0) return err(WG_EINVAL, "size beyond the maximum: term matrix too large");
+  if (!tile_rows_ok(st, m_max)) return err(WG_EINVAL, "size beyond the maximum: term matrix too large");
   bool all_odd = d.glynn != 0;
   for (int i = 0; i < E; ++i) all_odd = all_odd && (edge_reps[i] % 2 == 1);
   const WarpLayout L = make_layout(st, m_max, m_max, std::min(d.K, m_max), d.K + 2, 2,
                                    all_odd && d.K < m_max);
   const int wpc = std::min(8, (227 * 1024) / L.bytes);
   if (wpc < 1) return err(WG_EINVAL, "size beyond the maximum: per-warp workspace does not fit");
-  const int per_sm = sieve_occupancy(st, ns, wpc, wpc * L.bytes);
+  const int per_sm = sieve_occupancy(st, wpc, wpc * L.bytes);
   if (per_sm < 1) return err(WG_ECUDA, "sieve kernel cannot be resident");
   const long long resident = (long long)ds->sms * per_sm * wpc;
   long long nch = std::min<long long>(steps, 4 * resident);
@@ -231,7 +230,7 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   p.err = nullptr;
   p.L = L;
   const int ctas = (int)std::max<long long>(1, std::min<long long>((long long)ds->sms * per_sm, (nch + wpc - 1) / wpc));
-  const cudaError_t e = sieve_launch(st, ns, p, ctas, wpc, s);
+  const cudaError_t e = sieve_launch(st, p, ctas, wpc, s);
   if (e != cudaSuccess) return err(WG_ECUDA, "sieve kernel launch failed");
   reduce_kernel<<<1, 32, 0, s>>>(p.inst, 1, p.partials, reinterpret_cast<const double*>(scr + kOffScale),
                                  reinterpret_cast<double2*>(out_dev), p.counter, 1, 1, 0u);

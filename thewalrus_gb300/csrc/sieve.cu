@@ -5,7 +5,7 @@
 //     converted to the kernel's scalar type,
 //   * a chunk queue: every instance's term range split into chunks whose cost is balanced
 //     against the number of resident warps, largest instances first,
-//   * one persistent sieve launch per (scalar type, register class) group, and one reduction
+//   * one persistent sieve launch per (scalar type, resident warps per SM) group, and one reduction
 //     launch that sums chunk partials in a fixed order (bitwise reproducible results).
 #include <cuda_runtime.h>
 
@@ -17,7 +17,6 @@
 #include <map>
 #include <mutex>
 #include <string>
-#include <tuple>
 #include <vector>
 
 #include "../../include/walrus_gb300.h"
@@ -133,7 +132,7 @@ struct Prepared {
 };
 
 struct Group {
-  int stype, ns;
+  int stype;
   WarpLayout L;
   int wpc, ctas;
   int chunk_begin, chunk_count;
@@ -590,17 +589,17 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
   // (shared memory and registers decide how many CTAs fit), larger CTAs on ties -- e.g. 2 CTAs x
   // 7 warps where 1 x 8 would leave room unused.  {wpc, CTAs per SM}; wpc 0 when none fits.
   const int max_smem = 227 * 1024;
-  std::map<std::tuple<int, int, int>, std::pair<int, int>> shape_memo;
-  auto shape = [&](int st, int ns, int bytes) -> std::pair<int, int> {
-    const auto key = std::make_tuple(st, ns, bytes);
+  std::map<std::pair<int, int>, std::pair<int, int>> shape_memo;
+  auto shape = [&](int st, int bytes) -> std::pair<int, int> {
+    const auto key = std::make_pair(st, bytes);
     const auto it = shape_memo.find(key);
     if (it != shape_memo.end()) return it->second;
     const int wmax = std::min(wpc_cap, max_smem / bytes);
     std::pair<int, int> r{0, 0};
     if (wmax >= 1) {
-      int wpc = wmax, per_sm = sieve_occupancy(st, ns, wmax, wmax * bytes);
+      int wpc = wmax, per_sm = sieve_occupancy(st, wmax, wmax * bytes);
       for (int w = wmax - 1; w >= std::max(1, wmax / 2); --w) {
-        const int ps = sieve_occupancy(st, ns, w, w * bytes);
+        const int ps = sieve_occupancy(st, w, w * bytes);
         if (ps * w > per_sm * wpc) { wpc = w; per_sm = ps; }
       }
       r = {wpc, per_sm};
@@ -608,28 +607,26 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     shape_memo[key] = r;
     return r;
   };
-  // groups by (stype, ns, resident warps per SM of the instance's own workspace), so that a small
+  // groups by (stype, resident warps per SM of the instance's own workspace), so that a small
   // instance does not run at the occupancy of a larger one's workspace; with merge_classes one
-  // group per scalar type, at the largest class
-  struct GKey { int st, ns, res; };
+  // group per scalar type
+  struct GKey { int st, res; };
   std::vector<GKey> keys;
   std::vector<int> gid(count);
   for (int i = 0; i < count; ++i) {
-    const int ns = pick_ns(P[i].stype, P[i].rows_max);
-    if (ns < 0) return fail(WG_EINVAL, "instance %d: term matrix too large", i);
+    if (!tile_rows_ok(P[i].stype, P[i].rows_max)) return fail(WG_EINVAL, "instance %d: term matrix too large", i);
     int res = 0;
     if (!opt.merge_classes) {
       const WarpLayout Li = make_layout(P[i].stype, std::max(P[i].rows_max, 1), std::max(P[i].mb_max, 1),
                                         P[i].kc_max, std::max(P[i].nser_need, 2), std::max(P[i].narr, 2),
                                         P[i].tile_ok);
-      const auto sh = shape(P[i].stype, ns, Li.bytes);
+      const auto sh = shape(P[i].stype, Li.bytes);
       res = sh.first * sh.second;
     }
     int g = -1;
     for (size_t k = 0; k < keys.size(); ++k)
-      if (keys[k].st == P[i].stype && (opt.merge_classes || (keys[k].ns == ns && keys[k].res == res))) g = (int)k;
-    if (g < 0) { keys.push_back({P[i].stype, ns, res}); g = (int)keys.size() - 1; }
-    if (keys[g].ns < ns) keys[g].ns = ns;
+      if (keys[k].st == P[i].stype && (opt.merge_classes || keys[k].res == res)) g = (int)k;
+    if (g < 0) { keys.push_back({P[i].stype, res}); g = (int)keys.size() - 1; }
     gid[i] = g;
   }
   // pool
@@ -644,7 +641,6 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
   for (size_t g = 0; g < keys.size(); ++g) {
     Group G;
     G.stype = keys[g].st;
-    G.ns = keys[g].ns;
     int rows = 1, mb = 1, kc = 0, nser = 2, narr = 2;
     bool tile = true;
     double total_cost = 0;
@@ -662,7 +658,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
       }
     G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
     if (max_smem / G.L.bytes < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
-    const auto sh = shape(G.stype, G.ns, G.L.bytes);
+    const auto sh = shape(G.stype, G.L.bytes);
     const int wpc = sh.first, per_sm = sh.second;
     if (per_sm < 1) {
       cudaGetLastError();
@@ -820,7 +816,7 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
     p.err = pl->d_err;
     p.L = G.L;
     const cudaStream_t gs = (g == 0 || !side) ? st : pl->side[g - 1];
-    const cudaError_t e = sieve_launch(G.stype, G.ns, p, G.ctas, G.wpc, gs);
+    const cudaError_t e = sieve_launch(G.stype, p, G.ctas, G.wpc, gs);
     if (e != cudaSuccess) return fail(WG_ECUDA, "sieve launch: %s", cudaGetErrorString(e));
     if (g > 0 && side) {
       CK(cudaEventRecord(pl->side_done[g - 1], gs));

@@ -719,7 +719,7 @@ __device__ void loop_krylov(const S* __restrict__ W, int ldw, int m, int mb, int
 }
 
 // ------------------------------------------------------------------------------------------
-template <class S, int NS>
+template <class S>
 static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) {
   using A = Ar<S>;
   extern __shared__ __align__(16) unsigned char smem[];
