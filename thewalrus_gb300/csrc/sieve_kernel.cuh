@@ -190,23 +190,28 @@ __device__ __forceinline__ void neumaier(double& s, double& c, double x) {
 
 // Column j+1 of the elimination's similarity for rows lane + 32 k, k < NF (whole 32-row blocks):
 // W[a][j+1] = sum_{b=j+1}^{mb-1} W[a][b] x[b], one row per lane.
-template <class S, int NF>
-__device__ __forceinline__ void phase_b_rows(S* __restrict__ W, const S* __restrict__ xv, int ldw, int j, int mb) {
+// With PARTIAL the last block holds only the rows below `rows` (relative to W).
+template <class S, int NF, bool PARTIAL = false>
+__device__ __forceinline__ void phase_b_rows(S* __restrict__ W, const S* __restrict__ xv, int ldw, int j, int mb,
+                                             int rows = 0) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
   S acc[NF];
 #pragma unroll
   for (int k = 0; k < NF; ++k) acc[k] = A::zero();
+  const bool live = !PARTIAL || lane + 32 * (NF - 1) < rows;
   for (int b = j + 1; b < mb; ++b) {
     const S xb = xv[b];
 #pragma unroll
-    for (int k = 0; k < NF; ++k) acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], xb, acc[k]);
+    for (int k = 0; k < NF; ++k)
+      if (k < NF - 1 || live) acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], xb, acc[k]);
   }
 #pragma unroll
-  for (int k = 0; k < NF; ++k) W[(lane + 32 * k) * ldw + j + 1] = acc[k];
+  for (int k = 0; k < NF; ++k)
+    if (k < NF - 1 || live) W[(lane + 32 * k) * ldw + j + 1] = acc[k];
 }
 
-// The same for rows base .. rows-1 (fewer than 32, SL = ceil((rows - base) / 8) slots of 8):
+// The same for rows base .. rows-1 (at most 24, SL = ceil((rows - base) / 8) slots of 8):
 // lane = r8 + 8 c4 sums b = j+1+c4, j+5+c4, ... for rows base + r8 + 8 s, and a reduce-scatter
 // over the four column lanes (lane bits 3 and 4) leaves each row's total with one lane.
 template <class S, int SL>
@@ -370,8 +375,9 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
     __syncwarp();
     // --- phase B: W[a][j+1] = sum_{b=j+1}^{mb-1} W[a][b] x[b] for every row a < rows.  Whole
     // 32-row blocks take one row per lane, summed in b order (every lane busy, no cross-lane
-    // reduction); the rows after them (fewer than 32) take 8 row lanes x 4 column lanes over just
-    // the 8-row slots they fill, then a reduce-scatter over the column lanes.  The branches are
+    // reduction), and so does a last block of 25..31 rows; fewer rows after the whole blocks take
+    // 8 row lanes x 4 column lanes over just the 8-row slots they fill, then a reduce-scatter over
+    // the column lanes (cheaper there than a mostly idle row-per-lane block).  The branches are
     // warp-uniform, so no FP64 instruction is issued for an empty slot.
     const int nfull = rows >> 5;
     for (int k0 = 0; k0 < nfull; k0 += 2) {
@@ -379,13 +385,14 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
       else phase_b_rows<S, 1>(W + 32 * k0 * ldw, xv, ldw, j, mb);
     }
     const int rem = rows & 31;
-    if (rem > 0) {
+    if (rem >= 25) {
+      phase_b_rows<S, 1, true>(W + 32 * nfull * ldw, xv, ldw, j, mb, rem);
+    } else if (rem > 0) {
       const int base = rows - rem;
       switch ((rem + 7) >> 3) {
         case 1: phase_b_split<S, 1>(W, xv, ldw, j, mb, rows, base); break;
         case 2: phase_b_split<S, 2>(W, xv, ldw, j, mb, rows, base); break;
-        case 3: phase_b_split<S, 3>(W, xv, ldw, j, mb, rows, base); break;
-        default: phase_b_split<S, 4>(W, xv, ldw, j, mb, rows, base); break;
+        default: phase_b_split<S, 3>(W, xv, ldw, j, mb, rows, base); break;
       }
     }
     __syncwarp();
