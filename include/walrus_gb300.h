@@ -183,8 +183,9 @@ int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
  * callers that cannot allocate device memory while they call us -- code that runs inside its own
  * memory pool or arena, serving plugins that forbid allocation on the request path, and loops
  * where cudaMalloc/cudaFree would stall the device.  Same arguments and result as wg_hafnian,
- * except that A_dev (the prepared n x n matrix, n = 2E <= 64) and out_dev ({re, im}) are DEVICE
- * pointers on the current device, and the call only enqueues work on `stream` (synchronise
+ * except that A_dev (the prepared n x n matrix, n = 2E <= 64; 8-byte aligned) and
+ * out_dev ({re, im}; 16-byte aligned) are DEVICE pointers on the current device, and the call
+ * only enqueues work on `stream` (synchronise
  * before reading out_dev).  The working memory it needs beyond its inputs and outputs lives in
  * a static device array of WG_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
  * until the process exits; sizes beyond what the kernels or that array hold are rejected with

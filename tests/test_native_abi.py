@@ -97,3 +97,17 @@ def test_no_gpu_fails_loudly():
         pass
     with pytest.raises(RuntimeError):
         tw.hafnian(np.ones((6, 6)))
+
+
+def test_noalloc_rejects_misaligned_pointers():
+    # checked before any CUDA call: the kernels read A in 8-byte words and write the output pair
+    # in one 16-byte access (the pointer values are never dereferenced)
+    import ctypes
+    lib = nat.load()
+    reps = np.ones(3, dtype=np.int64)
+    rp = reps.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+    for A, dtype, out in ((0x10004, nat.WG_COMPLEX128, 0x20000), (0x10004, nat.WG_FLOAT64, 0x20000),
+                          (0x10000, nat.WG_COMPLEX128, 0x20008)):
+        rc = lib.wg_hafnian_noalloc(ctypes.c_void_p(A), 6, dtype, rp, 3, 1, ctypes.c_void_p(out), None)
+        assert rc == -1  # WG_EINVAL
+        assert b"aligned" in lib.wg_last_error()

@@ -14,13 +14,17 @@
 
 namespace wg {
 
+// The double-float scalars are aligned to their size, so that one moves in a single 128-bit
+// (64-bit for dfr) shared or global access (every tile, pool and series array is 16-byte
+// aligned): that took df n = 40 from 173 ms to 142 ms.  The same for c64 measured 1-3 % slower,
+// so it keeps the 8-byte alignment of its doubles.
 struct c64 {
   double re, im;
 };
-struct dfr {
+struct alignas(8) dfr {
   float hi, lo;
 };
-struct cdf {
+struct alignas(16) cdf {
   dfr re, im;
 };
 

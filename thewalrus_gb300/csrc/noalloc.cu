@@ -147,6 +147,9 @@ using namespace wg::noalloc;
 extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int64_t* edge_reps, int E, int glynn,
                                   double* out_dev, void* stream) {
   if (!A_dev || !out_dev || !edge_reps) return err(WG_EINVAL, "NULL argument");
+  // the kernels read A in 8-byte words and write the output pair in one 16-byte access
+  if (((uintptr_t)A_dev & 7u) != 0) return err(WG_EINVAL, "A must be 8-byte aligned");
+  if (((uintptr_t)out_dev & 15u) != 0) return err(WG_EINVAL, "out must be 16-byte aligned");
   if (dtype != WG_FLOAT64 && dtype != WG_COMPLEX128) return err(WG_EINVAL, "dtype must be WG_FLOAT64 or WG_COMPLEX128");
   if (E < 1 || n != 2 * E) return err(WG_EINVAL, "the prepared matrix must be 2E x 2E with E >= 1");
   if (E > MAX_EDGES)
