@@ -244,6 +244,24 @@ __device__ __forceinline__ void phase_b_split(S* __restrict__ W, const S* __rest
 #pragma unroll
   for (int i = NCOMP; i < NCP; ++i) v[i] = A::comp(A::zero(), 0);
   const bool h1 = (lane & 16) != 0, h2 = (lane & 8) != 0;
+  if constexpr (NCOMP <= 2) {
+    // one or two components: scatter them over lane bit 4 (two only), then a butterfly over bit 3
+    // -- two adds where the padded reduce-scatter below takes three
+    Comp z;
+    if constexpr (NCOMP == 2) {
+      const Comp send = h1 ? v[0] : v[1], keep = h1 ? v[1] : v[0];
+      z = A::cadd(keep, A::shfl_xor(send, 16));
+    } else {
+      z = A::cadd(v[0], A::shfl_xor(v[0], 16));
+    }
+    z = A::cadd(z, A::shfl_xor(z, 8));
+    __syncwarp();
+    const int vi = NCOMP == 2 && h1 ? 1 : 0;
+    const int s = vi / A::NC, part = vi % A::NC;
+    const int a = base + r8 + 8 * s;
+    if (!h2 && (NCOMP == 2 || !h1) && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z;
+    return;
+  }
   Comp u[NCP / 2];
 #pragma unroll
   for (int i = 0; i < NCP / 2; ++i) {
