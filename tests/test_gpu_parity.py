@@ -175,3 +175,23 @@ def test_all_ones_exact_to_n28():
             got = tw.hafnian(np.ones((n, n), dtype=dt), precision="fp64")
             assert round(got.real) == want and abs(got.imag) < 0.5, (n, dt, got, want)
             assert tw.hafnian(np.ones((n, n), dtype=dt)) == float(want)  # default: exact for integers
+
+
+@pytest.mark.parametrize("n,cplx", [(64, True), (58, True), (60, False)])
+def test_large_tiles_on_a_term_prefix(n, cplx):
+    """Term matrices of 58-64 rows (two whole 32-row blocks of the column update, or one block
+    and a 26-28-row block) on the first 64 sieve terms: those are the terms whose leading 25+
+    multiplicities sit at their first digit in both the Gray order here and the reference's
+    mixed-radix order, so the shard equals the oracle's term-range sum times 2^-(n/2-1)."""
+    from thewalrus_gb300 import _native as nat
+    P = 64
+    # the convention on a small instance first: the whole range is the hafnian
+    small = tw.prepare_hafnian(wl.complex_symmetric(12, seed=3))
+    whole = nat.run([small.shard(0, small.terms())])[0]
+    assert rel(whole, oracle.haf_term_range(small.A, small.reps, 0, small.terms()) * 2.0 ** -5) < RTOL
+    A = wl.complex_symmetric(n, seed=n) if cplx else wl.real_signed(n, seed=n)
+    inst = tw.prepare_hafnian(A)
+    assert inst.terms() == 2 ** (n // 2 - 1)
+    got = nat.run([inst.shard(0, P)])[0]
+    want = complex(oracle.haf_term_range(inst.A, inst.reps, 0, P)) * 2.0 ** -(n // 2 - 1)
+    assert rel(got, want) < 1e-9, (got, want)

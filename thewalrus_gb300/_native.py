@@ -273,7 +273,8 @@ class Plan:
     """Device-resident batch of instances: create once, execute many times, read results.
 
     ``chunk_scale`` (term-chunk size), ``max_warps_per_cta``, ``merge_classes`` (one persistent
-    launch per scalar type) and ``use_graph`` (CUDA-graph replay) map to ``wg_plan_options``.
+    launch per scalar type), ``use_graph`` (CUDA-graph replay) and ``serial_groups`` (launch the
+    groups one after another on the caller's stream) map to ``wg_plan_options``.
     """
 
     def __init__(self, instances, precision="fp64", chunk_scale=1.0, max_warps_per_cta=0,
@@ -309,8 +310,8 @@ class Plan:
             arr[i] = WgRequest(xa.ctypes.data, ra.ctypes.data, len(ra), -1 if odd is None else int(odd))
         self._keep, self._arr = keep, arr
         opt = WgPlanOptions(float(options.get("chunk_scale", 1.0)), int(options.get("max_warps_per_cta", 0)),
-                            int(bool(options.get("merge_classes", False))), int(bool(options.get("use_graph", False))), 0,
-                            options.get("stream"))
+                            int(bool(options.get("merge_classes", False))), int(bool(options.get("use_graph", False))),
+                            int(bool(options.get("serial_groups", False))), options.get("stream"))
         h = ctypes.c_void_p()
         check(self.lib.wg_plan_create_requests(state.handle, arr, len(requests), PRECISIONS[precision],
                                                ctypes.byref(opt), ctypes.byref(h)))
