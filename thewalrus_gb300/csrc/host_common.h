@@ -182,17 +182,14 @@ static inline bool lb_schedule(int Ki, LbLane* lanes, LbOwner* own) {
   return false;
 }
 
-// Two-row steady-state schedule for K coefficients: the pieces of both rows' r-sums (each j's
-// j-1 products cut into ceil((j-1)/t) runs, per row) packed into 32 lanes, at most three pieces
-// per lane, largest first onto the least-loaded lane that fits; smallest feasible t.
-static inline bool lb_schedule2(int K0, int K1, LbLane2* lanes, LbOwner2* own) {
+// One packing of the two-row r-sums at per-lane load t.  split_once = false: the sums longest
+// first, poured into the lanes in order, a sum split where a lane fills.  split_once = true:
+// each sum of t or more products gives whole lanes of t, and its remainder joins the shorter
+// sums, packed first-fit longest first -- every coefficient then has at most two pieces.  At most
+// three pieces per lane and seven per coefficient; false when that does not fit in 32 lanes.
+static inline bool lb2_pack(int K0, int K1, int t, bool split_once, LbLane2* lanes, LbOwner2* own) {
   for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
   for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
-  if (K0 < 0 || K1 < K0 || K1 > LB2_KMAX) return false;
-  const int W = K0 * (K0 - 1) / 2 + K1 * (K1 - 1) / 2;
-  if (W == 0) return true;
-  // the r-sums (row, j) longest first, poured into the lanes in order: a lane closes when it
-  // holds t products or four pieces, and a sum that crosses a lane boundary is split there
   struct Sum { int row, j, len; };
   Sum sums[2 * (LB2_KMAX + 1)];
   int ns = 0;
@@ -204,38 +201,98 @@ static inline bool lb_schedule2(int K0, int K1, LbLane2* lanes, LbOwner2* own) {
     while (y >= 0 && sums[y].len < key.len) { sums[y + 1] = sums[y]; --y; }
     sums[y + 1] = key;
   }
-  for (int t = std::max(1, (W + 31) / 32); t <= 64; ++t) {
-    for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
-    for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
-    int lane = 0, load = 0, npc = 0;
-    bool ok = true;
-    for (int q = 0; q < ns && ok; ++q) {
+  int load[32] = {0}, npc[32] = {0};
+  // piece (row, j, r .. r+len-1) into lane l
+  auto put = [&](int l, const Sum& sm, int r, int len) -> bool {
+    if (l >= 32 || npc[l] >= 3 || load[l] + len > t) return false;
+    LbLane2& L = lanes[l];
+    const int q = npc[l]++;
+    L.j[q] = (signed char)sm.j;
+    L.rlo[q] = (signed char)r;
+    L.len[q] = (signed char)len;
+    if (sm.row) L.rowmask |= (unsigned char)(1u << q);
+    load[l] += len;
+    LbOwner2& o = own[sm.j];
+    unsigned char& n = sm.row ? o.n1 : o.n0;
+    unsigned char* sl = sm.row ? o.s1 : o.s0;
+    if (n >= 7) return false;
+    sl[n++] = (unsigned char)(3 * l + q);
+    return true;
+  };
+  if (!split_once) {
+    int lane = 0;
+    for (int q = 0; q < ns; ++q) {
       int r = 1, left = sums[q].len;
-      while (left > 0 && ok) {
-        if (load == t || npc == 3) { ++lane; load = 0; npc = 0; }
-        if (lane >= 32) { ok = false; break; }
-        const int take = std::min(left, t - load);
-        LbLane2& L = lanes[lane];
-        L.j[npc] = (signed char)sums[q].j;
-        L.rlo[npc] = (signed char)r;
-        L.len[npc] = (signed char)take;
-        if (sums[q].row) L.rowmask |= (unsigned char)(1u << npc);
-        LbOwner2& o = own[sums[q].j];
-        unsigned char& n = sums[q].row ? o.n1 : o.n0;
-        unsigned char* sl = sums[q].row ? o.s1 : o.s0;
-        if (n >= 7) { ok = false; break; }
-        sl[n++] = (unsigned char)(3 * lane + npc);
-        ++npc;
-        load += take;
+      while (left > 0) {
+        if (lane < 32 && (load[lane] == t || npc[lane] == 3)) ++lane;
+        if (lane >= 32) return false;
+        const int take = std::min(left, t - load[lane]);
+        if (!put(lane, sums[q], r, take)) return false;
         r += take;
         left -= take;
       }
     }
-    if (ok) return true;
+    return true;
   }
-  for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
+  int next = 0;  // first lane never used
+  Sum rest[2 * (LB2_KMAX + 1)];
+  int rlo[2 * (LB2_KMAX + 1)];
+  int nr = 0;
+  for (int q = 0; q < ns; ++q) {
+    int r = 1, left = sums[q].len;
+    while (left >= t) {
+      if (!put(next++, sums[q], r, t)) return false;
+      r += t;
+      left -= t;
+    }
+    if (left > 0) { rest[nr] = {sums[q].row, sums[q].j, left}; rlo[nr++] = r; }
+  }
+  for (int x = 1; x < nr; ++x) {  // remainders and short sums, stable longest first
+    const Sum key = rest[x];
+    const int kr = rlo[x];
+    int y = x - 1;
+    while (y >= 0 && rest[y].len < key.len) { rest[y + 1] = rest[y]; rlo[y + 1] = rlo[y]; --y; }
+    rest[y + 1] = key;
+    rlo[y + 1] = kr;
+  }
+  for (int x = 0; x < nr; ++x) {
+    int l = 0;
+    while (l < 32 && !(npc[l] < 3 && load[l] + rest[x].len <= t)) ++l;
+    if (l >= 32 || !put(l, rest[x], rlo[x], rest[x].len)) return false;
+  }
+  return true;
+}
+
+// Two-row schedule (rows i and i+1 of La Budde with K0 and K1 coefficients): of both packings
+// at every per-lane load t from the smallest possible up, the one with the least kernel cost --
+// 4 x the largest lane load (product iterations of four FP64 instructions, complex) plus 2 x the
+// most pieces of any coefficient of each row (the owner pass's subtractions).
+static inline bool lb_schedule2(int K0, int K1, LbLane2* lanes, LbOwner2* own) {
   for (int l = 0; l < 32; ++l) lanes[l] = LbLane2{{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, 0, {0, 0}};
-  return false;
+  for (int j = 0; j <= LB2_KMAX; ++j) own[j] = LbOwner2{0, 0, {0}, {0}};
+  if (K0 < 0 || K1 < K0 || K1 > LB2_KMAX) return false;
+  const int W = K0 * (K0 - 1) / 2 + K1 * (K1 - 1) / 2;
+  if (W == 0) return true;
+  LbLane2 tl[32];
+  LbOwner2 to[LB2_KMAX + 1];
+  int best = -1;
+  const int t0 = std::max(1, (W + 31) / 32);
+  for (int t = t0; t <= 64; ++t) {
+    for (int mode = 0; mode < 2; ++mode) {
+      if (!lb2_pack(K0, K1, t, mode == 1, tl, to)) continue;
+      int mx = 0, m0 = 0, m1 = 0;
+      for (int l = 0; l < 32; ++l) mx = std::max(mx, tl[l].len[0] + tl[l].len[1] + tl[l].len[2]);
+      for (int j = 0; j <= K1; ++j) { m0 = std::max(m0, (int)to[j].n0); m1 = std::max(m1, (int)to[j].n1); }
+      const int cost = 4 * mx + 2 * (m0 + m1);
+      if (best < 0 || cost < best) {
+        best = cost;
+        std::copy(tl, tl + 32, lanes);
+        std::copy(to, to + LB2_KMAX + 1, own);
+      }
+    }
+    if (best >= 0 && 4 * t >= best) break;  // loads near t cost 4t or more: stop the search
+  }
+  return best >= 0;
 }
 
 // every two-row table: lanes[LB2_IDS * 32], own[LB2_IDS * (LB2_KMAX + 1)], entry lb2_id(K0, K1)
