@@ -1,7 +1,8 @@
 """Autotuner for batched sieve plans.
 
-Chooses the term-chunk size (chunks per resident warp), the warps per CTA and whether uneven
-instances share one persistent launch per scalar type, by timing candidate plans on the GPU.
+Chooses the term-chunk size (chunks per resident warp), the warps per CTA, whether uneven
+instances share one persistent launch per scalar type and whether the launches run one after
+another or overlap on side streams, by timing candidate plans on the GPU.
 Results are cached per (GPU, precision, workload signature) in ``_build/autotune.json`` next to
 the native library, so a workload shape is tuned once per machine.
 
