@@ -230,6 +230,17 @@ def main():
         put("gbs_threshold", cov=cov, mean=mean, seed=77, fanout=4, cutoff=1, max_photons=30, count=4,
             out=samples, next_uniform=np.random.random_sample())
 
+    # graph states (quantum/adjacency_matrices.py, conversions.py): scaling, Q and covariance
+    from thewalrus.quantum import adj_scaling, gen_Qmat_from_graph, Covmat
+    grng = np.random.default_rng(61)
+    for n, n_mean, weighted in ((6, 2.0, False), (8, 5.0, True), (5, 0.7, True)):
+        G = np.triu((grng.random((n, n)) < 0.5).astype(float), 1)
+        if weighted:
+            G = G * grng.uniform(0.2, 1.5, size=(n, n))
+        A = G + G.T
+        Q = gen_Qmat_from_graph(A, n_mean)
+        put("graph", A=A, n_mean=n_mean, scale=adj_scaling(A, n_mean), Q=Q, cov=Covmat(Q))
+
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
     print("wrote %d arrays for %s in %.1fs" % (len(out), counts, time.time() - t0))
 

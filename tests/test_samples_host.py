@@ -44,3 +44,19 @@ def test_permutation_helpers():
     assert np.array_equal(smp.invert_permutation(p)[p], np.arange(4))
     mu = np.arange(6.0)
     assert np.allclose(smp.mu_to_alpha(mu, hbar=2), (mu[:3] + 1j * mu[3:]) / 2)
+
+
+def test_graph_state_vs_reference(golden):
+    # adj_scaling / gen_Qmat_from_graph / Covmat of the graph samplers against the reference's
+    for c in golden["graph"]:
+        A, n_mean = c["A"], float(c["n_mean"])
+        x = smp.adj_scaling(A, n_mean)
+        assert abs(x - float(c["scale"])) <= 1e-11 * abs(float(c["scale"]))
+        Q = smp.gen_Qmat_from_graph(A, n_mean)
+        assert np.allclose(Q, c["Q"], atol=1e-10, rtol=1e-10)
+        cov = smp.Covmat(Q)
+        assert np.allclose(cov, c["cov"], atol=1e-10, rtol=1e-10)
+        # the state is pure and carries the requested mean photon number
+        n = len(A)
+        assert abs((np.trace(cov) - 2 * n) / 4 - n_mean) < 1e-8
+        assert abs(np.linalg.det(cov) - 1.0) < 1e-7

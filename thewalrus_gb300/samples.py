@@ -2,6 +2,9 @@
 
 Drop-ins for ``thewalrus.samples.generate_hafnian_sample``, ``hafnian_sample_state``,
 ``generate_torontonian_sample`` and ``torontonian_sample_state`` (thewalrus/samples.py:95-590),
+and the graph forms ``hafnian_sample_graph`` / ``torontonian_sample_graph`` (:372-399, :591-621:
+the pure Gaussian state that encodes an adjacency matrix at a given mean photon number, then the
+state samplers),
 the callers of ``loop_hafnian_batch`` and ``loop_hafnian_batch_gamma``.  For mode k = 1..M the
 sampler evaluates the loop hafnians of the first k modes for every photon number 0..cutoff of
 mode k (one batch sieve, the earlier modes fixed at their sampled counts), turns them into
@@ -38,6 +41,11 @@ __all__ = [
     "hafnian_sample_state",
     "generate_torontonian_sample",
     "torontonian_sample_state",
+    "adj_scaling",
+    "gen_Qmat_from_graph",
+    "Covmat",
+    "hafnian_sample_graph",
+    "torontonian_sample_graph",
 ]
 
 
@@ -307,3 +315,71 @@ def torontonian_sample_state(cov, samples, mu=None, hbar=2, max_photons=30, fano
         if res != -1:
             got.append(res)
     return np.vstack(got)
+
+
+# ---------------------------------------------------------------------------------------------
+# Graph states (thewalrus/quantum/adjacency_matrices.py:90-177, conversions.py:99-121)
+
+
+def adj_scaling(A, n_mean):
+    """The factor x for which the pure Gaussian state encoding x A has mean photon number
+    ``n_mean``: sum_i (x s_i)^2 / (1 - (x s_i)^2) = n_mean over the singular values s_i of A,
+    solved by bracketed root finding on (0, 1 / s_max) (adjacency_matrices.py:90-152)."""
+    from scipy.optimize import brentq
+
+    eps = 1e-10
+    s = np.linalg.svd(np.asarray(A), compute_uv=False)
+    if 1000 * eps >= s[0]:
+        raise ValueError("The singular values of the matrix A are too small.")
+
+    def excess(x):
+        v = (x * s) ** 2
+        return float(np.sum(v / (1.0 - v))) - n_mean
+
+    return brentq(excess, 0.0, 1.0 / (eps + s[0]), xtol=2e-12, rtol=4 * np.finfo(float).eps, maxiter=200)
+
+
+def gen_Qmat_from_graph(A, n_mean):
+    """Husimi Q matrix of the pure state encoding the adjacency matrix A at mean photon number
+    ``n_mean``: Q = (I - X (x A (+) conj(x A)))^-1 with X the mode-swap block matrix
+    (adjacency_matrices.py:155-177)."""
+    A = np.asarray(A)
+    n, m = A.shape
+    if n != m:
+        raise ValueError("Matrix must be square.")
+    Asc = adj_scaling(A, n_mean) * A
+    Z = np.zeros_like(Asc)
+    B = np.block([[Asc, Z], [Z, Asc.conj()]])
+    idn = np.identity(n)
+    X = np.block([[0 * idn, idn], [idn, 0 * idn]])
+    return np.linalg.inv(np.identity(2 * n) - X @ B)
+
+
+def Covmat(Q, hbar=2):
+    """xp-ordered Wigner covariance matrix of the state with Husimi matrix Q
+    (conversions.py:99-121)."""
+    n = len(Q) // 2
+    idn = np.identity(n)
+    N = Q[0:n, 0:n] - idn
+    M = Q[n:2 * n, 0:n]
+    c11 = 2 * (N.real + M.real) + idn
+    c22 = 2 * (N.real - M.real) + idn
+    c12 = 2 * (M.imag + N.imag)
+    return (hbar / 2) * np.block([[c11, c12], [c12.T, c22]])
+
+
+def hafnian_sample_graph(A, n_mean, samples=1, cutoff=5, max_photons=30, parallel=False, precision=None):
+    """Photon-number samples of the pure state encoding the adjacency matrix A at mean photon
+    number ``n_mean`` (thewalrus/samples.py:372-399)."""
+    cov = Covmat(gen_Qmat_from_graph(A, n_mean), hbar=2)
+    return hafnian_sample_state(cov, samples, mean=None, hbar=2, cutoff=cutoff, max_photons=max_photons,
+                                parallel=parallel, precision=precision)
+
+
+def torontonian_sample_graph(A, n_mean, samples=1, max_photons=30, fanout=10, cutoff=1, parallel=False,
+                             precision=None):
+    """Click samples of the pure state encoding the adjacency matrix A at mean photon number
+    ``n_mean`` (thewalrus/samples.py:591-621)."""
+    cov = Covmat(gen_Qmat_from_graph(A, n_mean), hbar=2)
+    return torontonian_sample_state(cov, samples, hbar=2, max_photons=max_photons, fanout=fanout, cutoff=cutoff,
+                                    parallel=parallel, precision=precision)
