@@ -53,3 +53,21 @@ def test_threshold_samples_vs_reference(golden):
                                            cutoff=int(c["cutoff"]), max_photons=int(c["max_photons"]))
         assert np.array_equal(got, c["out"]), (got, c["out"])
         assert np.random.random_sample() == float(c["next_uniform"])
+
+
+def test_graph_samplers_are_the_state_samplers_of_the_graph_state(golden):
+    # the graph forms build the pure state of the scaled adjacency matrix (checked against the
+    # reference on the CPU) and hand it to the state samplers with hbar = 2 and no displacement
+    c = golden["graph"][0]
+    A, n_mean = c["A"], float(c["n_mean"])
+    cov = smp.Covmat(smp.gen_Qmat_from_graph(A, n_mean))
+    np.random.seed(5)
+    got = smp.hafnian_sample_graph(A, n_mean, samples=3, cutoff=5, max_photons=20)
+    np.random.seed(5)
+    want = smp.hafnian_sample_state(cov, 3, cutoff=5, max_photons=20)
+    assert np.array_equal(got, want) and got.shape == (3, len(A))
+    np.random.seed(6)
+    got = smp.torontonian_sample_graph(A, n_mean, samples=2, fanout=3)
+    np.random.seed(6)
+    want = smp.torontonian_sample_state(cov, 2, fanout=3)
+    assert np.array_equal(got, want) and got.shape == (2, len(A))
