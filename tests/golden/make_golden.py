@@ -241,6 +241,18 @@ def main():
         Q = gen_Qmat_from_graph(A, n_mean)
         put("graph", A=A, n_mean=n_mean, scale=adj_scaling(A, n_mean), Q=Q, cov=Covmat(Q))
 
+    # density-matrix elements of mixed, displaced and undisplaced states (fock_tensors.py:191-232)
+    from thewalrus.quantum import density_matrix_element
+    drng = np.random.default_rng(71)
+    M = 3
+    U = wl.haar_unitary(M, np.random.default_rng(72))
+    S = sy.interferometer(U) @ sy.squeezing(drng.uniform(0.2, 0.6, size=M))
+    for k, (thermal, disp) in enumerate(((0.0, 0.0), (0.4, 0.0), (0.4, 0.5), (0.0, 0.5))):
+        cov = S @ S.T + thermal * np.eye(2 * M)
+        mu = drng.normal(size=2 * M) * disp
+        for i, j in (([1, 0, 1], [1, 0, 1]), ([2, 1, 0], [0, 1, 2]), ([0, 0, 0], [1, 1, 0]), ([3, 0, 1], [1, 2, 1])):
+            put("dm", mu=mu, cov=cov, i=np.array(i), j=np.array(j), out=density_matrix_element(mu, cov, i, j))
+
     np.savez_compressed(os.path.join(HERE, "reference_cases.npz"), **out)
     print("wrote %d arrays for %s in %.1fs" % (len(out), counts, time.time() - t0))
 
