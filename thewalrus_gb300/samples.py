@@ -249,7 +249,7 @@ def hafnian_sample_state(cov, samples, mean=None, hbar=2, cutoff=5, max_photons=
     chain = _Chain(cov, mean, hbar)
     got = []
     while len(got) < samples:
-        # every attempt of this round is one the sequential reference would also make
+        # every attempt of this pass is one the sequential reference would also make
         for res in _hafnian_attempts(chain, samples - len(got), cutoff, max_photons,
                                      precision or DEFAULT_PRECISION):
             if res != -1:
