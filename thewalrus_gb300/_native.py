@@ -57,25 +57,31 @@ def build(force=False, verbose=False):
         tag = "%d" % os.getpid()
         compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
         procs, objs = [], []
-        for src in SOURCES:  # translation units compile in parallel, then one link
-            obj = os.path.join(BUILD, src.replace(".cu", ".%s.o" % tag))
-            cmd = [_nvcc()] + compile_flags + ["-c", os.path.join(CSRC, src), "-o", obj]
-            procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
-            objs.append(obj)
-        for cmd, p in procs:
-            out, _ = p.communicate()
-            if p.returncode != 0:
-                raise RuntimeError("nvcc failed:\n%s\n%s" % (" ".join(cmd), out.decode()))
-            if verbose and out:
-                print(out.decode())
         tmp = LIB + ".tmp" + tag
-        cmd = [_nvcc(), "-shared", "-o", tmp] + objs
-        res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
-        if res.returncode != 0:
-            raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), res.stdout.decode()))
-        for obj in objs:
-            os.unlink(obj)
-        os.replace(tmp, LIB)
+        try:
+            for src in SOURCES:  # translation units compile in parallel, then one link
+                obj = os.path.join(BUILD, src.replace(".cu", ".%s.o" % tag))
+                cmd = [_nvcc()] + compile_flags + ["-c", os.path.join(CSRC, src), "-o", obj]
+                procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+                objs.append(obj)
+            failed = None
+            for cmd, p in procs:  # wait for every compiler before reporting the first failure
+                out, _ = p.communicate()
+                if p.returncode != 0 and failed is None:
+                    failed = "nvcc failed:\n%s\n%s" % (" ".join(cmd), out.decode())
+                elif verbose and out:
+                    print(out.decode())
+            if failed:
+                raise RuntimeError(failed)
+            cmd = [_nvcc(), "-shared", "-o", tmp] + objs
+            res = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+            if res.returncode != 0:
+                raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), res.stdout.decode()))
+            os.replace(tmp, LIB)
+        finally:  # no object or half-written library outlives the build, failed or not
+            for path in objs + [tmp]:
+                if os.path.exists(path):
+                    os.unlink(path)
         return LIB
 
 
