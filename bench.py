@@ -132,32 +132,60 @@ class ClockSampler:
 
 
 def run_reference(args, rank, world):
+    """The reference arm: whole n=40 hafnians by the CPU restatement of the reference algorithm
+    on all host cores.  One hafnian takes ~28 s on 16 cores, so at most ``BENCH_REF_STEPS``
+    (default 3) whole hafnians are timed, whatever ``--steps`` asks, and no warm-up runs (a C
+    library has no JIT to warm); the line states both."""
     if rank != 0:
         return
+    import numpy as np
+
+    import oracle
+
     threads = os.cpu_count() or 1
-    rates = []
-    info = None
-    per_step = float(os.environ.get("BENCH_REF_STEP_SECONDS", "6"))
-    for i in range(args.warmup + args.steps):
-        r, info = cpu_sample(seconds=per_step, threads=threads)
-        if i >= args.warmup:
-            rates.append(r)
-    value = statistics.mean(rates)
-    sample = ("terms [0, %d) of the %d-term n=40 sieve per step, C restatement of the reference "
-              "algorithm (double, %d threads), scaled to whole hafnians" %
-              (info["terms"], info["total_terms"], threads))
+    steps = max(1, min(args.steps, int(os.environ.get("BENCH_REF_STEPS", "3"))))
+    A = workload()
+    secs = []
+    result = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        result = complex(oracle.hafnian(A, nthreads=threads))
+        secs.append(time.perf_counter() - t0)
+    value = steps / sum(secs)
+    sample = ("%d whole hafnians (all %d sieve terms each), C restatement of the reference algorithm "
+              "(mixed-radix terms, matrix-power traces; double, %d threads)" % (steps, 2 ** (N_MATRIX // 2 - 1),
+                                                                                 threads))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
+        "steps": steps, "warmup": 0, "steps_requested": args.steps, "warmup_requested": args.warmup,
+        "ms_per_step": 1e3 * sum(secs) / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": value * PUBLISHED_N40_SECONDS, "dtype": "f64",
         "data": "synthetic",
         "config": {"workload": "hafnian 40x40 complex128 (G+G^T)/2, seed 0, 524288 sieve terms",
                    "precision": "fp64", "parallelism": "%d host threads" % threads},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "result": [result.real, result.imag],
     }
+    ref = metric_reference("haf40_complex")
+    if ref is not None:
+        line["rel_err_vs_reference"] = abs(result - ref[0]) / abs(ref[0])
     print(json.dumps(line), flush=True)
+
+
+def metric_reference(case):
+    """(value the reference's own code produced, long-double oracle value) for a benchmark input,
+    from the committed fixture tests/golden/metric_cases.npz; None when the fixture is absent."""
+    import numpy as np
+
+    path = os.path.join(ROOT, "tests", "golden", "metric_cases.npz")
+    if not os.path.exists(path):
+        return None
+    data = np.load(path)
+    if case + "/out" not in data.files:
+        return None
+    ld = data[case + "/oracle_ld"] if case + "/oracle_ld" in data.files else None
+    return complex(data[case + "/out"]), (None if ld is None else complex(ld))
 
 
 def run_gpu(args, rank, world, local):
@@ -230,13 +258,6 @@ def run_gpu(args, rank, world, local):
     mean_s = total_ms / args.steps * 1e-3
     achieved = flops / mean_s / 1e12
     peak = fp64_peak if args.precision == "fp64" else fp32_peak
-    # DRAM bytes per sieve launch from the committed ncu capture of this workload (FP64, n = 40)
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "sieve_c64_n40_traffic.md")
-    if n == N_MATRIX and args.precision == "fp64" and os.path.exists(prof):
-        for ln in open(prof):
-            if ln.startswith("bytes_per_launch:"):
-                traffic = float(ln.split(":", 1)[1])
     if rank != 0:
         return
     line = {
@@ -254,7 +275,8 @@ def run_gpu(args, rank, world, local):
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": None,
+                     "traffic_note": "DRAM bytes need an ncu capture, not taken inside the bench",
                      "peak_source": "FMA-pipe microbenchmark (wg_measure_fp_peaks) in this run",
                      "flops_per_launch": flops},
         "gpu_launches": args.steps * plan.kernel_launches,
@@ -265,6 +287,12 @@ def run_gpu(args, rank, world, local):
     if n != N_MATRIX or args.matrix != "complex":
         line["metric"] = "n=%d hafnians/s (%s, Glynn sieve)" % (
             n, "complex128" if args.matrix == "complex" else "float64")
+    ref = metric_reference("haf40_complex" if args.matrix == "complex" else "haf40_real") if n == N_MATRIX else None
+    if ref is not None:
+        line["rel_err_vs_reference"] = abs(complex(result) - ref[0]) / abs(ref[0])
+        if ref[1] is not None:
+            line["rel_err_vs_oracle_ld"] = abs(complex(result) - ref[1]) / abs(ref[1])
+        line["e2e_rel_err_vs_reference"] = abs(complex(r) - ref[0]) / abs(ref[0])
     if not args.no_cpu_baseline and n == N_MATRIX and args.matrix == "complex":
         rate, info = cpu_sample(seconds=args.cpu_seconds)
         line["cpu_baseline"] = {
@@ -272,8 +300,127 @@ def run_gpu(args, rank, world, local):
             "sample": "terms [0, %d) of the %d-term sieve in %.1f s, C restatement of the reference "
                       "algorithm in double on %d threads" % (info["terms"], info["total_terms"],
                                                              info["seconds"], info["threads"])}
-    print(json.dumps(line), flush=True)
     plan.close()
+    if world == 1 and not args.no_extras and n == N_MATRIX and args.matrix == "complex":
+        line["batch"] = batch_summary(args)
+        line["serve"] = serve_summary(args)
+    print(json.dumps(line), flush=True)
+
+
+def batch_summary(args):
+    """Batching (a stated subset of the 4096-instance workload): every 16th of the 4096 uneven
+    instances (n in 8..40, half real non-negative, half complex) plus the 16 loop_hafnian_batch
+    calls (12 modes, cutoff 6), as one autotuned, graph-replayed plan against the same instances
+    through the public API one call each; accuracy of the batched results against the
+    long-double oracle on the members with n <= 20."""
+    import numpy as np
+    import torch
+
+    import oracle
+    import thewalrus_gb300 as tw
+    from thewalrus_gb300 import _native as nat, autotune, workloads as wl
+
+    mats = wl.batch_instances(count=4096, seed=2)[::16]
+    calls = wl.batch_loop_calls(count=16, seed=3, modes=12, cutoff=6)
+    insts = [tw.prepare_hafnian(A) for A in mats] + \
+        [tw.prepare_loop_hafnian_batch(B, D, list(f), c) for B, D, f, c in calls]
+    cands = [{"chunk_scale": cs, "max_warps_per_cta": 0, "merge_classes": mc, "serial_groups": False}
+             for cs in (1.0, 2.0, 4.0) for mc in (False, True)]
+    t0 = time.perf_counter()
+    best, _ = autotune.tune(insts[::4], precision="fp64", candidates=cands, repeats=1, use_cache=False)
+    tune_s = time.perf_counter() - t0
+    plan = nat.Plan(insts, precision="fp64", use_graph=True, **best)
+    s = torch.cuda.current_stream()
+    plan.execute(s.cuda_stream)  # captures the graph
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        plan.execute(s.cuda_stream)
+        e1.record(s)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    batched_s = statistics.median(times)
+    got = plan.read(s.cuda_stream)
+    plan.close()
+    outputs = len(mats) + sum(int(c) + 1 for _, _, _, c in calls)
+    t0 = time.perf_counter()
+    per = [tw.hafnian(A, precision="fp64") for A in mats]
+    per_b = [tw.loop_hafnian_batch(B, D, list(f), c, precision="fp64") for B, D, f, c in calls]
+    per_call_s = time.perf_counter() - t0
+    diff = max(abs(per[i] - got[i]) / abs(per[i]) for i in range(len(mats)))
+    off = len(mats)
+    for b in per_b:
+        diff = max(diff, float(np.max(np.abs(b - got[off:off + len(b)])) / np.max(np.abs(b))))
+        off += len(b)
+    err = 0.0
+    checked = 0
+    for i, A in enumerate(mats):
+        if len(A) <= 20:
+            want = complex(oracle.hafnian(A, precision="long"))
+            err = max(err, abs(got[i] - want) / abs(want))
+            checked += 1
+    return {"workload": "every 16th of the 4096 uneven hafnians (%d, n in 8..40) + 16 loop_hafnian_batch "
+                        "(12 modes, cutoff 6; %d outputs): one autotuned plan, CUDA-graph replay" % (len(mats), outputs - len(mats)),
+            "hafnians_per_s": outputs / batched_s, "seconds": batched_s,
+            "per_call_hafnians_per_s": outputs / per_call_s, "per_call_seconds": per_call_s,
+            "speedup_vs_per_call": per_call_s / batched_s,
+            "max_rel_diff_vs_per_call": diff, "max_rel_err_vs_oracle_ld": err, "oracle_checked": checked,
+            "autotuned": best, "autotune_seconds": tune_s, "kernel_launches": plan.kernel_launches}
+
+
+def serve_summary(args):
+    """Serving (Poisson streams of probability requests on four 64-mode Gaussian states, patterns
+    of 8-44 photons, at most 2 per mode): p50/p99 latency and hafnians/s at two arrival rates with
+    ``--serve-count`` requests each; the higher rate's requests also one call each (matrices
+    formed on the device, one plan per request, synchronous); loop hafnians of the requests with
+    at most 24 photons against the long-double oracle."""
+    import numpy as np
+
+    import oracle
+    from thewalrus_gb300 import _native as nat
+    from thewalrus_gb300._hafnian import matched_reps
+    from thewalrus_gb300.serving import GaussianState, ProbabilityServer, poisson_requests, summary
+
+    states = [GaussianState.synthetic(modes=64, seed=s) for s in range(4)]
+    srv = ProbabilityServer(states, precision="fp64", max_batch=256, streams=3)
+    srv.serve(poisson_requests(states, 1e6, 16, photons=(8, 16), seed=99))  # warm-up
+    rows = []
+    err, checked = 0.0, 0
+    for rate in args.serve_rates:
+        # one seed for every rate: the same requests (states, patterns), arrival times scaled by 1/rate
+        reqs = poisson_requests(states, rate, args.serve_count, photons=(8, 44), seed=7)
+        t0 = time.perf_counter()
+        res = srv.serve(reqs)
+        span = time.perf_counter() - t0
+        sm = summary(res, makespan=span)
+        sm["rate"] = rate
+        rows.append(sm)
+        for (t, sidx, pat), r in zip(reqs, res):
+            if np.sum(pat) <= 24 and checked < 64:
+                st = states[sidx]
+                want = complex(oracle.hafnian_repeated(st.B, list(pat), mu=st.gamma, loop=True, precision="long"))
+                lhaf = r["amplitude"] / st.norm(pat)
+                err = max(err, abs(lhaf - want) / abs(want))
+                checked += 1
+    done = 0
+    t0 = time.perf_counter()
+    for _, sidx, pat in reqs:
+        if states[sidx].trivial_loop_hafnian(pat) is not None:
+            continue
+        plan = nat.Plan.from_requests(states[sidx].device, [matched_reps(pat)], "fp64")
+        plan.execute()
+        plan.read()
+        plan.close()
+        done += 1
+    srv.torch.cuda.synchronize()
+    per_call_s = time.perf_counter() - t0
+    return {"workload": "%d requests per rate, Poisson arrivals, 4 synthetic 64-mode pure states, 8-44 photons"
+                        % args.serve_count,
+            "rates": rows, "per_call": {"requests": done, "seconds": per_call_s, "hafnians_per_s": done / per_call_s,
+                                        "same_requests_as_rate": args.serve_rates[-1]},
+            "max_rel_err_vs_oracle_ld": err, "oracle_checked": checked}
 
 
 def _gpu_setup(local=0):
@@ -411,7 +558,7 @@ def run_serve(args):
     srv.serve(poisson_requests(states, 1e6, 8, photons=(lo, min(hi, lo + 8)), seed=99))  # warm-up
     rows = []
     for rate in args.rates:
-        reqs = poisson_requests(states, rate, args.serve_count, photons=(lo, hi), seed=int(rate))
+        reqs = poisson_requests(states, rate, args.serve_count, photons=(lo, hi), seed=7)
         t0 = time.perf_counter()
         res = srv.serve(reqs)
         span = time.perf_counter() - t0
@@ -446,8 +593,16 @@ def run_serve(args):
 
 
 def run_precision(args):
-    """Relative error of FP64 and double-float sieve terms against the _Float128 oracle (n <= 24)
-    and exact integer rounding for 0/1 adjacency matrices; the n=48 classes are timed."""
+    """Precision of the three term arithmetics: FP64, FP32 double-float and FP64 double-double.
+
+    * n = 20 (``--precision-n``), ``--precision-seeds`` seeds per class: against the _Float128
+      oracle.
+    * n = 48, the large-size table: random 0/1 graphs (edge probability 0.5) and integer
+      non-negative matrices (rint(|G| + |G|^T)) against their exact hafnians (the exact sieve over
+      residues, pinned against the CPU modular oracle), ``--precision-seeds48`` seeds each;
+      signed real and complex matrices against the double-double sieve (pinned against the
+      _Float128 oracle to 1e-20 at n <= 20), ``--precision-dd-seeds`` seeds (half that for the
+      complex class, whose double-double run takes minutes).  Times per hafnian per mode."""
     import numpy as np
 
     torch, nat = _gpu_setup()
@@ -455,49 +610,55 @@ def run_precision(args):
     import thewalrus_gb300 as tw
     from thewalrus_gb300 import workloads as wl
 
+    def stats(v):
+        return {"max": float(np.max(v)), "median": float(np.median(v)), "seeds": len(v)}
+
     gens = {"complex": wl.complex_symmetric, "real_signed": wl.real_signed, "real_nonneg": wl.real_nonneg,
             "adjacency01": wl.adjacency01}
-    table = {}
+    small = {}
     for name, gen in gens.items():
-        errs = {"fp64": [], "df": []}
+        errs = {"fp64": [], "df": [], "dd": []}
         for seed in range(args.precision_seeds):
             A = gen(args.precision_n, seed=seed)
             ref = complex(oracle.hafnian(A, precision="quad"))
-            for p in ("fp64", "df"):
+            for p in errs:
                 g = tw.hafnian(A, precision=p)
                 errs[p].append(abs(g - ref) / abs(ref) if ref != 0 else abs(g))
-                if name == "adjacency01" and p == "fp64":
-                    assert round(g.real) == round(ref.real)
-        table[name] = {p: {"max": float(np.max(v)), "median": float(np.median(v))} for p, v in errs.items()}
-    # 0/1 graphs against the exact modular oracle (integer counts): n = 32 (counts ~ 2^41) and
-    # n = 40 (~ 2^58, beyond FP64's integers)
-    exact_rows = {}
-    for n, seeds in ((32, range(args.precision_seeds)), (40, range(2))):
+        small[name] = {p: stats(v) for p, v in errs.items()}
+
+    def timed(A, p):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        v = tw.hafnian(A, precision=p)
+        return complex(v), time.perf_counter() - t0
+
+    n = 48
+    large = {}
+    classes = [("adjacency01", lambda sd: wl.adjacency01(n, seed=sd), "exact", args.precision_seeds48),
+               ("int_nonneg", lambda sd: np.rint(wl.real_nonneg(n, seed=sd)), "exact", args.precision_seeds48 // 4),
+               ("real_signed", lambda sd: wl.real_signed(n, seed=sd), "dd", args.precision_dd_seeds),
+               ("complex", lambda sd: wl.complex_symmetric(n, seed=sd), "dd", max(1, args.precision_dd_seeds // 2))]
+    for name, gen, truth_mode, seeds in classes:
         errs = {"fp64": [], "df": []}
+        secs = {"fp64": [], "df": [], truth_mode: []}
         rounds = 0
-        for seed in seeds:
-            A = wl.adjacency01(n, seed=seed)
-            ref = oracle.exact_hafnian(A)
-            for p in ("fp64", "df"):
-                g = tw.hafnian(A, precision=p)
-                errs[p].append(abs(complex(g) - ref) / ref)
-                if p == "fp64":
-                    rounds += int(round(g.real) == ref)
-        exact_rows["adjacency01_n%d" % n] = {
-            "seeds": len(errs["fp64"]), "fp64_rounds_exactly": rounds,
-            **{p: {"max": float(np.max(v)), "median": float(np.median(v))} for p, v in errs.items()}}
-    table["exact_integer"] = exact_rows
-    timing = {}
-    for name, gen in gens.items():
-        A = gen(48, seed=0)
-        for p in ("fp64", "df"):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            tw.hafnian(A, precision=p)
-            timing["%s/%s" % (name, p)] = time.perf_counter() - t0
-    print(json.dumps({"metric": "relative error vs _Float128 oracle (n=%d, %d seeds per class) and vs exact counts (0/1 graphs)"
-                      % (args.precision_n, args.precision_seeds), "errors": table,
-                      "n48_seconds_per_hafnian": timing}), flush=True)
+        for seed in range(seeds):
+            A = gen(seed)
+            truth, dt = timed(A, truth_mode)
+            secs[truth_mode].append(dt)
+            for p in errs:
+                v, dt = timed(A, p)
+                secs[p].append(dt)
+                errs[p].append(abs(v - truth) / abs(truth))
+                if truth_mode == "exact" and p == "fp64":
+                    rounds += int(round(v.real) == truth.real)
+        row = {"truth": truth_mode, **{p: stats(v) for p, v in errs.items()},
+               "seconds_per_hafnian": {p: float(np.median(v)) for p, v in secs.items()}}
+        if truth_mode == "exact":
+            row["fp64_rounds_to_the_integer"] = rounds
+        large[name] = row
+    print(json.dumps({"metric": "relative error of FP64 / double-float / double-double sieve terms",
+                      "n%d_vs_float128_oracle" % args.precision_n: small, "n48": large}), flush=True)
 
 
 def run_sample(args):
@@ -570,14 +731,19 @@ def main():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batch and serve sub-objects of the default line")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 20000.0])
     ap.add_argument("--workload", choices=["n40", "loop", "batch", "serve", "precision", "sample"], default="n40",
                     help="n40: the benchmark line; the others report the other configurations")
     ap.add_argument("--batch-count", type=int, default=4096)
     ap.add_argument("--rates", type=float, nargs="+", default=[100.0, 1000.0, 5000.0, 20000.0])
-    ap.add_argument("--serve-count", type=int, default=64)
+    ap.add_argument("--serve-count", type=int, default=512)
     ap.add_argument("--photons", type=int, nargs=2, default=[8, 44])
     ap.add_argument("--precision-n", type=int, default=20)
     ap.add_argument("--precision-seeds", type=int, default=8)
+    ap.add_argument("--precision-seeds48", type=int, default=64)
+    ap.add_argument("--precision-dd-seeds", type=int, default=8)
     ap.add_argument("--sample-modes", type=int, default=12)
     ap.add_argument("--samples", type=int, default=256)
     args = ap.parse_args()

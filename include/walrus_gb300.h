@@ -31,6 +31,10 @@ extern "C" {
 /* arithmetic of the sieve terms */
 #define WG_PREC_FP64 0 /* FP64 throughout */
 #define WG_PREC_DF 1   /* FP32 double-float terms; FP64 pivots, divisions and accumulation */
+/* FP64 double-double terms (106-bit significand) and compensated accumulation that keeps each
+ * term's low part: for sums whose terms cancel beyond what FP64 resolves (sum|term| / |sum|
+ * above ~1e6).  About 15-20x the FP64 time.  Not offered for serving plans. */
+#define WG_PREC_DD 7
 /* Exact sieve of an integer-valued float64 instance modulo the prime WG_MOD_PRIME_k (entries and
  * loop weights integers of magnitude below 2^31): every output is a residue in [0, p), returned
  * in the real part; residues of several primes give the exact integer by the Chinese remainder
@@ -189,7 +193,9 @@ int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
  * before reading out_dev).  The working memory it needs beyond its inputs and outputs lives in
  * a static device array of WG_NOALLOC_SCRATCH_BYTES that every GPU loading this library keeps
  * until the process exits; sizes beyond what the kernels or that array hold are rejected with
- * WG_EINVAL.  The first call on a device sets the array up (make it before any stream capture).
+ * WG_EINVAL, and so are edge repetitions that are all zero (no photons: the hafnian is 1, a
+ * closed form the caller answers).  The first call on a device sets the array up (make it
+ * before any stream capture).
  * All calls share the array: calls that overlap on the GPU race, so serialise them. */
 #define WG_NOALLOC_SCRATCH_BYTES (512 * 1024)
 int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int64_t* edge_reps, int E, int glynn,

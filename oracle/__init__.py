@@ -62,6 +62,9 @@ def _load():
             f = getattr(lib, "oracle_hafnian_term_range" + sfx)
             f.argtypes = [dp, ctypes.c_int, ip, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                           ctypes.c_int64, ctypes.c_int64, dp]
+            f = getattr(lib, "oracle_sieve_term_range" + sfx)
+            f.argtypes = [ctypes.c_int, dp, dp, ctypes.c_int, ip, ctypes.c_int, dp, dp, ctypes.c_int,
+                          ctypes.c_int, ctypes.c_int64, ctypes.c_int64, ctypes.c_int, dp]
             f = getattr(lib, "oracle_powertrace" + sfx)
             f.argtypes = [dp, ctypes.c_int, ctypes.c_int, dp]
             f = getattr(lib, "oracle_charpoly" + sfx)
@@ -161,6 +164,27 @@ def haf_term_range(Ax, edge_reps, t_begin, t_end, glynn=True, precision="double"
     getattr(lib, "oracle_hafnian_term_range" + _SFX[precision])(
         pA, A.shape[0], pr, len(r), int(bool(glynn)), nthreads or _default_threads(),
         int(t_begin), int(t_end), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return DD(*_dd(out))
+
+
+def sieve_term_range(Ax, edge_reps, t_begin=0, t_end=-1, Dx=None, oddloop=None, oddV=None, glynn=True,
+                     absolute=False, precision="double", nthreads=None):
+    """Unscaled sum over the terms [t_begin, t_end) (t_end = -1: to the end) of the plain
+    (``Dx`` None) or loop sieve on prepared inputs, in the reference's mixed-radix term order;
+    ``absolute=True`` sums the terms' absolute values instead (with the absolute value of the
+    scaled sum this gives the sum's condition number)."""
+    lib = _load()
+    A, pA = _cbuf(Ax)
+    r, pr = _ibuf(edge_reps)
+    kind = 0 if Dx is None else (2 if oddloop is not None else 1)
+    D, pD = _cbuf(Dx if Dx is not None else np.zeros(1))
+    V, pV = _cbuf(oddV if oddV is not None else np.zeros(1))
+    ol = np.array([complex(oddloop or 0).real, complex(oddloop or 0).imag])
+    out = np.zeros(4)
+    getattr(lib, "oracle_sieve_term_range" + _SFX[precision])(
+        kind, pA, pD, A.shape[0], pr, len(r), ol.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), pV,
+        int(bool(glynn)), nthreads or _default_threads(), int(t_begin), int(t_end), int(bool(absolute)),
+        out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     return DD(*_dd(out))
 
 

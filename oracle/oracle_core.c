@@ -409,7 +409,8 @@ static void FN(store_dd)(C v, double* out) {
 /* The sum over sieve terms.  Each thread sums a contiguous range; the thread partials are then
  * added in thread order.  `kind`: 0 plain, 1 loop (even), 2 loop with odd self-loop. */
 static C FN(sieve)(int kind, const C* A, const C* D, int n, const int64_t* reps, int E, C oddloop,
-                   const C* oddV, int glynn, int nthreads, int64_t t_begin, int64_t t_end, int scale) {
+                   const C* oddV, int glynn, int nthreads, int64_t t_begin, int64_t t_end, int scale,
+                   int absmode) {
   int N = 0;
   for (int i = 0; i < E; ++i) N += 2 * (int)reps[i];
   if (kind == 2) N += 1;
@@ -470,7 +471,10 @@ static C FN(sieve)(int kind, const C* A, const C* D, int n, const int64_t* reps,
         memcpy(AXc, AXS, sizeof(C) * m * m);
         val = FN(f_loop_odd)(AXc, AXS, XDS, DS, m, N, oddloop, OV, &w, pt, comb, v1, v2);
       }
-      acc = FN(cadd)(acc, FN(cscale)(val, prefac));
+      if (absmode) /* sum of |prefac * term|: the sum's condition number is that over |sum| */
+        acc.re += FN(cabs_)(FN(cscale)(val, prefac));
+      else
+        acc = FN(cadd)(acc, FN(cscale)(val, prefac));
     }
     partial[tid] = acc;
     FN(ws_free)(&w);
@@ -497,7 +501,7 @@ int FN(oracle_calc_hafnian)(const double* A, int n, const int64_t* edge_reps, in
                             int nthreads, double* out) {
   C* Ac = (C*)malloc(sizeof(C) * (n > 0 ? n * n : 1));
   FN(load_c)(A, Ac, (size_t)n * n);
-  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads, 0, -1, 1);
+  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads, 0, -1, 1, 0);
   FN(store_dd)(h, out);
   free(Ac);
   return 0;
@@ -508,7 +512,7 @@ int FN(oracle_hafnian_term_range)(const double* A, int n, const int64_t* edge_re
                                   int nthreads, int64_t t_begin, int64_t t_end, double* out) {
   C* Ac = (C*)malloc(sizeof(C) * (n > 0 ? n * n : 1));
   FN(load_c)(A, Ac, (size_t)n * n);
-  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads, t_begin, t_end, 0);
+  C h = FN(sieve)(0, Ac, NULL, n, edge_reps, E, FN(cmk)(0, 0), NULL, glynn, nthreads, t_begin, t_end, 0, 0);
   FN(store_dd)(h, out);
   free(Ac);
   return 0;
@@ -527,7 +531,30 @@ int FN(oracle_calc_loop_hafnian)(const double* A, const double* D, int n, const 
     FN(load_c)(oddV, Vc, (size_t)n);
     ol = FN(cmk)((R)oddloop[0], (R)oddloop[1]);
   }
-  C h = FN(sieve)(has_odd ? 2 : 1, Ac, Dc, n, edge_reps, E, ol, has_odd ? Vc : NULL, glynn, nthreads, 0, -1, 1);
+  C h = FN(sieve)(has_odd ? 2 : 1, Ac, Dc, n, edge_reps, E, ol, has_odd ? Vc : NULL, glynn, nthreads, 0, -1, 1, 0);
+  FN(store_dd)(h, out);
+  free(Ac); free(Dc); free(Vc);
+  return 0;
+}
+
+/* Partial sums over sieve terms [t_begin, t_end) (mixed-radix order) of the plain or loop sieve,
+ * unscaled, for checks and conditioning: kind 0 plain, 1 loop, 2 loop with an odd self-loop;
+ * absmode 1 returns the sum of the terms' absolute values in the real part instead. */
+int FN(oracle_sieve_term_range)(int kind, const double* A, const double* D, int n, const int64_t* edge_reps,
+                                int E, const double* oddloop, const double* oddV, int glynn, int nthreads,
+                                int64_t t_begin, int64_t t_end, int absmode, double* out) {
+  C* Ac = (C*)malloc(sizeof(C) * (n > 0 ? n * n : 1));
+  C* Dc = (C*)malloc(sizeof(C) * (n > 0 ? n : 1));
+  C* Vc = (C*)malloc(sizeof(C) * (n > 0 ? n : 1));
+  FN(load_c)(A, Ac, (size_t)n * n);
+  if (kind > 0) FN(load_c)(D, Dc, (size_t)n);
+  C ol = FN(cmk)(0, 0);
+  if (kind == 2) {
+    FN(load_c)(oddV, Vc, (size_t)n);
+    ol = FN(cmk)((R)oddloop[0], (R)oddloop[1]);
+  }
+  C h = FN(sieve)(kind, Ac, kind > 0 ? Dc : NULL, n, edge_reps, E, ol, kind == 2 ? Vc : NULL, glynn, nthreads,
+                  t_begin, t_end, 0, absmode);
   FN(store_dd)(h, out);
   free(Ac); free(Dc); free(Vc);
   return 0;

@@ -1,17 +1,36 @@
 """Generate golden input/output vectors from the reference implementation itself.
 
-Run in a container that has the reference source checked out (default ``/root/reference``,
-override with ``WALRUS_REFERENCE``).  numba is not needed: a stub module turns ``numba.jit``
-into the identity and ``numba.prange`` into ``range``, so the reference's own Python code runs
-as plain NumPy.  The package ``__init__`` (which pulls in dask) is bypassed by registering a bare
-``thewalrus`` package whose path is the reference's source directory.
+Usage::
+
+    python tests/golden/make_golden.py REFERENCE_CHECKOUT            # small cases
+    python tests/golden/make_golden.py REFERENCE_CHECKOUT --metric   # benchmark-size cases
+    python tests/golden/make_golden.py --metric-oracle   # re-run only their oracle cross-check
+
+``REFERENCE_CHECKOUT`` is a source checkout of thewalrus (the directory holding the
+``thewalrus`` package); the environment variable ``WALRUS_REFERENCE`` may give it instead.
+numba is not needed: a stub module turns ``numba.jit`` into the identity and ``numba.prange``
+into ``range``, so the reference's own Python code runs as plain NumPy.  The package
+``__init__`` (which pulls in dask) is bypassed by registering a bare ``thewalrus`` package whose
+path is the reference's source directory.
+
+``--metric`` evaluates the benchmark-size inputs (the 40x40 complex and real plain hafnians,
+seed 0, and the 20-mode, 40-photon Gaussian-state loop hafnian) through the reference's public
+``hafnian`` / ``hafnian_repeated``.  Single-threaded that is ~1 ms per sieve term (524,288 terms
+for n = 40), so the work is split over processes: in each worker the stub's ``prange(steps)``
+yields only one slice of the term range, the reference's own ``_calc_hafnian`` /
+``_calc_loop_hafnian`` sum that slice (their result is linear in the sum: the final
+``0.5 ** (N/2 - 1)`` scale applies to each slice alike) and the slices' results are added in
+term order with ``math.fsum``.  Output: ``metric_cases.npz``.
 
 One reference quirk is guarded: ``charpoly.powertrace`` of a 0x0 matrix indexes an empty array
 (thewalrus/charpoly.py:215-217); the guard returns the values the reference's loops produce
 around that read (p_0 = 0 followed by zeros).
 
-Output: ``reference_cases.npz`` next to this script.  Keys are ``<family>/<index>/<field>``.
+Output of the default mode: ``reference_cases.npz`` next to this script.  Keys are
+``<family>/<index>/<field>``.
 """
+import math
+import multiprocessing as mp
 import os
 import sys
 import time
@@ -25,7 +44,13 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from thewalrus_gb300 import workloads as wl  # noqa: E402
 
 
+_IMPORTED = {}
+
+
 def import_reference(path):
+    if path in _IMPORTED:
+        return _IMPORTED[path]
+
     def mk(name):
         m = types.ModuleType(name)
         m.__path__ = []
@@ -72,11 +97,120 @@ def import_reference(path):
         return orig(H, n)
 
     cp.powertrace = guarded
+    _IMPORTED[path] = (cp, hf, lb, ref)
     return cp, hf, lb, ref
 
 
-def main():
-    path = os.environ.get("WALRUS_REFERENCE", "/root/reference")
+def _slice_worker(args):
+    """Evaluate one slice [p/P, (p+1)/P) of the reference's sieve loop through its public API."""
+    path, case, piece, pieces = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    cp, hf, lb, ref = import_reference(path)
+
+    def prange(steps):
+        return range(steps * piece // pieces, steps * (piece + 1) // pieces)
+
+    # the reference modules keep the numba stub they were imported with (a worker process runs
+    # several slices), so patch that module object
+    hf.numba.prange = prange
+    kind, A, extra = case
+    if kind == "haf":
+        val = hf.hafnian(A)
+    else:
+        rpt, mu = extra
+        val = hf.hafnian_repeated(A, list(rpt), mu=mu, loop=True)
+    return piece, complex(val)
+
+
+def metric_cases(path, workers=None, pieces=256):
+    """Benchmark-size reference values (see the module docstring), split over processes."""
+    cases = {
+        "haf40_complex": ("haf", wl.complex_symmetric(40, seed=0), None),
+        "haf40_real": ("haf", wl.real_signed(40, seed=0), None),
+    }
+    A, gamma, rpt = wl.gaussian_state_loop(modes=20, seed=1, photons=40, max_rep=3)
+    cases["lhaf_state20_40"] = ("lhaf", A, (rpt, gamma))
+    workers = workers or os.cpu_count()
+    out = {}
+    ctx = mp.get_context("spawn")
+    for name, case in cases.items():
+        t0 = time.time()
+        with ctx.Pool(workers) as pool:
+            parts = sorted(pool.map(_slice_worker, [(path, case, p, pieces) for p in range(pieces)]))
+        val = complex(math.fsum(v.real for _, v in parts), math.fsum(v.imag for _, v in parts))
+        kind, A, extra = case
+        out[name + "/A"] = A
+        if extra is not None:
+            out[name + "/rpt"] = np.asarray(extra[0])
+            out[name + "/mu"] = np.asarray(extra[1])
+        out[name + "/out"] = np.asarray(val)
+        print("%s = %r (%.0f s on %d processes)" % (name, val, time.time() - t0, workers), flush=True)
+    np.savez_compressed(os.path.join(HERE, "metric_cases.npz"), **out)
+    metric_oracle_check()
+
+
+def metric_oracle_check():
+    """Cross-check of ``metric_cases.npz`` with the oracle, adding per case (fields already
+    present are kept):
+
+    * ``oracle_ld``: the long-double oracle's value (x87 80-bit on x86-64);
+    * ``cond``: the sieve sum's condition number sum|term| / |sum| (double oracle), the factor
+      by which per-term rounding reaches the result;
+    * ``oracle_q``: the _Float128 oracle's value, for the cases whose ``cond`` exceeds 1e6 (there
+      even the long-double result has only ~1e-19 * cond relative accuracy).
+    """
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import oracle
+    import thewalrus_gb300 as tw
+
+    path = os.path.join(HERE, "metric_cases.npz")
+    data = dict(np.load(path))
+    for name in sorted({k.split("/")[0] for k in data}):
+        A = data[name + "/A"]
+        ref = complex(data[name + "/out"])
+        loop = name + "/rpt" in data
+
+        def value(precision):
+            if loop:
+                return complex(oracle.hafnian_repeated(A, list(data[name + "/rpt"]), mu=data[name + "/mu"],
+                                                       loop=True, precision=precision))
+            return complex(oracle.hafnian(A, precision=precision))
+
+        if name + "/cond" not in data:
+            t0 = time.time()
+            if loop:
+                p = tw.prepare_loop_hafnian(A, data[name + "/mu"], list(data[name + "/rpt"]))
+                tot = oracle.sieve_term_range(p.A, p.reps, Dx=p.D, absolute=True)
+                N = int(2 * np.sum(p.reps))
+            else:
+                p = tw.prepare_hafnian(A)
+                tot = oracle.sieve_term_range(p.A, p.reps, absolute=True)
+                N = int(2 * np.sum(p.reps))
+            cond = complex(tot).real * 0.5 ** (N // 2 - 1) / abs(ref)
+            data[name + "/cond"] = np.asarray(cond)
+            print("%s: condition number %.3g (%.0f s)" % (name, cond, time.time() - t0), flush=True)
+        for key, precision in (("oracle_ld", "long"), ("oracle_q", "quad")):
+            if name + "/" + key in data or (key == "oracle_q" and float(data[name + "/cond"]) <= 1e6):
+                continue
+            t0 = time.time()
+            val = value(precision)
+            data[name + "/" + key] = np.asarray(val)
+            print("%s: oracle (%s) %r, relative difference from the reference %.2e (%.0f s)"
+                  % (name, precision, val, abs(val - ref) / abs(ref), time.time() - t0), flush=True)
+            np.savez_compressed(path, **data)
+    np.savez_compressed(path, **data)
+
+
+def reference_path(argv):
+    args = [a for a in argv if not a.startswith("--")]
+    path = args[0] if args else os.environ.get("WALRUS_REFERENCE")
+    if not path:
+        raise SystemExit("usage: make_golden.py REFERENCE_CHECKOUT [--metric] "
+                         "(or set WALRUS_REFERENCE)")
+    return path
+
+
+def main(path):
     cp, hf, lb, ref = import_reference(path)
     rng = np.random.default_rng(20261203)
     out = {}
@@ -258,4 +392,9 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if "--metric-oracle" in sys.argv[1:]:
+        metric_oracle_check()
+    elif "--metric" in sys.argv[1:]:
+        metric_cases(reference_path(sys.argv[1:]))
+    else:
+        main(reference_path(sys.argv[1:]))

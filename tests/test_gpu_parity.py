@@ -195,3 +195,24 @@ def test_large_tiles_on_a_term_prefix(n, cplx):
     got = nat.run([inst.shard(0, P)])[0]
     want = complex(oracle.haf_term_range(inst.A, inst.reps, 0, P)) * 2.0 ** -(n // 2 - 1)
     assert rel(got, want) < 1e-9, (got, want)
+
+
+def test_golden_families_double_float(golden):
+    """Every golden family with FP32 double-float terms (48-bit significand): 1e-8 relative, the
+    bound the double-float error table supports at these sizes (n <= 24, worst seen 1.2e-9 on a
+    signed real n = 20 matrix)."""
+    tol = 1e-8
+    for c in golden["haf"]:
+        assert rel(tw.hafnian(c["A"], precision="df"), c["out"]) < tol, c["A"].shape
+    for c in golden["haf_inclexcl"]:
+        assert rel(tw.hafnian(c["A"], method="inclexcl", precision="df"), c["out"]) < tol
+    for c in golden["lhaf"]:
+        assert rel(tw.hafnian(c["A"], loop=True, precision="df"), c["out"]) < tol, c["A"].shape
+    for c in golden["rep"]:
+        assert rel(tw.hafnian_repeated(c["A"], list(c["rpt"]), precision="df"), c["out"]) < tol
+    for c in golden["rep_loop"]:
+        got = tw.hafnian_repeated(c["A"], list(c["rpt"]), mu=c["mu"], loop=True, precision="df")
+        assert rel(got, c["out"]) < tol, c["rpt"]
+    for c in golden["batch"]:
+        got = tw.loop_hafnian_batch(c["A"], c["D"], list(c["fixed"]), int(c["cutoff"]), precision="df")
+        assert np.max(np.abs(got - c["out"])) / np.max(np.abs(c["out"])) < tol

@@ -2,6 +2,7 @@
 reference test-suite's known answers (thewalrus/tests/test_hafnian.py, test_hafnian_repeated.py,
 test_labudde.py, test_reference.py)."""
 import math
+import os
 
 import numpy as np
 import pytest
@@ -140,3 +141,22 @@ def test_exact_oracle_known_values():
     # against the _Float128 oracle on a 20-vertex graph
     A = wl.adjacency01(20, seed=4)
     assert oracle.exact_hafnian(A) == round(complex(oracle.hafnian(A, precision="quad")).real)
+
+
+def test_metric_fixture_cross_checks():
+    """The benchmark-size reference values (tests/golden/metric_cases.npz) against the oracle's
+    values stored beside them: the well-conditioned plain hafnians agree to 1e-12; the loop
+    hafnian of the 20-mode, 40-photon state (condition number ~3e10) agrees with the _Float128
+    value within 2^-53 times its condition number."""
+    data = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "metric_cases.npz"))
+    for case in ("haf40_complex", "haf40_real"):
+        out, ld = complex(data[case + "/out"]), complex(data[case + "/oracle_ld"])
+        assert abs(out - ld) <= 1e-12 * abs(ld)
+        assert float(data[case + "/cond"]) < 1e6
+    out = complex(data["lhaf_state20_40/out"])
+    q = complex(data["lhaf_state20_40/oracle_q"])
+    ld = complex(data["lhaf_state20_40/oracle_ld"])
+    cond = float(data["lhaf_state20_40/cond"])
+    assert cond > 1e9
+    assert abs(out - q) <= 2.0 ** -53 * cond * abs(q)
+    assert abs(ld - q) <= 2.0 ** -64 * cond * abs(q)

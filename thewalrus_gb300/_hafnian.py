@@ -51,6 +51,18 @@ def _integral(inst):
     return len(inst.reps) == 0 or int(np.max(inst.reps)) <= 50
 
 
+def _integer_valued(*arrays):
+    """True when every given array (or scalar) holds real integers: such inputs take the exact
+    sieve by default, whose result no scaling could improve."""
+    for a in arrays:
+        if a is None:
+            continue
+        a = np.asarray(a)
+        if a.size and (np.iscomplexobj(a) and np.any(a.imag != 0) or np.any(np.real(a) != np.round(np.real(a)))):
+            return False
+    return True
+
+
 def _auto(precision, insts):
     """The precision of a call: the caller's, else exact for integer inputs (the sieve over
     residues modulo 31-bit primes, so integer hafnians come back exactly, rounded once to
@@ -129,6 +141,61 @@ def _is_complex(*arrays):
     return any(a is not None and np.iscomplexobj(a) and np.any(np.asarray(a).imag != 0) for a in arrays)
 
 
+def _pair_balance(Ax, Dx=None, oddV=None, first=0, spread=16.0, sweeps=16):
+    """Balance a prepared matrix by a similarity that leaves every sieve term unchanged.
+
+    In a prepared matrix vertex e is matched to vertex E + e.  Scaling vertex e by s_e and
+    vertex E + e by 1/s_e (A -> S A S, loop weights D -> S D, the odd vertex's row oddV -> S oddV)
+    multiplies the hafnian of the expanded matrix by prod_e (s_e / s_e)^r_e = 1, and each sieve
+    term's matrix A X_delta by the diagonal similarity S (.) S^-1, so no term changes either.
+    Such a scaling can make rows of one column differ by many orders of magnitude, which the
+    term matrices' pivoted Hessenberg reduction meets as tiny pivots and threshold-size
+    candidates; the reference's matrix-power traces are indifferent to it.  Choosing s_e (powers
+    of two, so the scaling is exact) so that the paired rows e and E + e get equal absolute row
+    sums undoes it: a few sweeps of that rule are Parlett-Reinsch balancing of the term matrix
+    restricted to pair scalings.  Edges before ``first`` (the batch edge, and in the odd batch
+    form the edge of the odd mode, whose unpaired copies would carry the scale) stay unscaled.
+    Returns the scaled (Ax, Dx, oddV), or None when every pair's row sums already agree within
+    ``spread`` (the usual case: inputs are then used exactly as given)."""
+    n = Ax.shape[0]
+    E = n // 2
+    if E - first < 1:
+        return None
+    w = np.abs(Ax.real) + np.abs(Ax.imag)
+    if Dx is not None:
+        w = np.concatenate([w, (np.abs(Dx.real) + np.abs(Dx.imag))[:, None]], axis=1)
+    rows = w.sum(axis=1)
+    e = np.arange(first, E)
+    a, b = rows[e], rows[e + E]
+    ok = (a > 0) & (b > 0)
+    if not np.any(ok) or np.all((a[ok] <= spread * b[ok]) & (b[ok] <= spread * a[ok])):
+        return None
+    k = np.zeros(n, dtype=np.int64)  # log2 of each vertex's scale
+    for _ in range(sweeps):
+        moved = False
+        for i in range(first, E):
+            d = np.ldexp(1.0, k)
+            dw = d[:, None] * w[:, :n] * d[None, :]
+            ra = dw[i].sum() + (d[i] * w[i, n] if Dx is not None else 0.0)
+            rb = dw[i + E].sum() + (d[i + E] * w[i + E, n] if Dx is not None else 0.0)
+            if ra <= 0 or rb <= 0:
+                continue
+            step = int(np.round(0.5 * np.log2(rb / ra)))
+            if step:
+                k[i] += step
+                k[i + E] -= step
+                moved = True
+        if not moved:
+            break
+    if not np.any(k):
+        return None
+    d = np.ldexp(1.0, k)
+    Ax = d[:, None] * Ax * d[None, :]
+    Dx = None if Dx is None else d * Dx
+    oddV = None if oddV is None else d * oddV
+    return Ax, Dx, oddV
+
+
 def prepare_hafnian(A, reps=None, glynn=True):
     """Host preparation of ``_haf``: returns a native instance, or a plain value when the
     sieve is not needed (no photons: 1.0; odd photon number: 0.0)."""
@@ -143,6 +210,10 @@ def prepare_hafnian(A, reps=None, glynn=True):
     x, edge_reps, _ = matched_reps(reps)
     Ax = A[np.ix_(x, x)]
     Ax = _cast(Ax, np.complex128 if _is_complex(Ax) else np.float64)
+    if not _integer_valued(Ax):  # integer inputs run the exact sieve, which needs no balancing
+        bal = _pair_balance(Ax)
+        if bal is not None:
+            Ax = bal[0]
     return nat.Instance(nat.WG_KIND_PLAIN, Ax, edge_reps, glynn=glynn)
 
 
@@ -169,6 +240,10 @@ def prepare_loop_hafnian(A, D=None, reps=None, glynn=True):
         oddloop, oddV = None, None
     Ax = _cast(A[np.ix_(x, x)], dt)
     Dx = _cast(np.asarray(D)[x], dt)
+    if not _integer_valued(Ax, Dx, oddV, oddloop):
+        bal = _pair_balance(Ax, Dx, oddV)
+        if bal is not None:
+            Ax, Dx, oddV = bal
     return nat.Instance(nat.WG_KIND_LOOP, Ax, edge_reps, glynn=glynn, D=Dx, oddV=oddV, oddloop=oddloop)
 
 
@@ -309,6 +384,10 @@ def prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True):
         edges = _batch_edges_odd(fixed_edges, oddmode)
     Ax = _cast(Anz[np.ix_(edges, edges)], dt)
     Dx = _cast(Dnz[edges], dt)
+    if not _integer_valued(Ax, Dx):  # the batch edge (and the odd mode's edge) stay unscaled
+        bal = _pair_balance(Ax, Dx, first=1 if oddmode is None else 2)
+        if bal is not None:
+            Ax, Dx = bal[0], bal[1]
     return nat.Instance(kind, Ax, fixed_m_reps, glynn=glynn, D=Dx, batch_max=batch_max, cutoff=cutoff)
 
 

@@ -16,17 +16,18 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libwalrus_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["sieve.cu", "noalloc.cu", "kernels_c64.cu", "kernels_cdf.cu", "kernels_f64.cu", "kernels_fdf.cu",
-           "kernels_mod0.cu", "kernels_mod1.cu", "kernels_mod2.cu", "kernels_mod3.cu", "kernels_mod4.cu"]
+           "kernels_cdd.cu", "kernels_fdd.cu", "kernels_mod0.cu", "kernels_mod1.cu", "kernels_mod2.cu",
+           "kernels_mod3.cu", "kernels_mod4.cu"]
 DEPS = SOURCES + ["sieve_kernel.cuh", "arith.cuh", "host_common.h", "kernels.h", "kernels_unit.cuh"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-shared"]
 
 WG_FLOAT64, WG_COMPLEX128 = 0, 1
-WG_PREC_FP64, WG_PREC_DF = 0, 1
+WG_PREC_FP64, WG_PREC_DF, WG_PREC_DD = 0, 1, 7
 WG_PREC_MOD = (2, 3, 4, 5, 6)
 MOD_PRIMES = (2147483647, 2147483629, 2147483587, 2147483579, 2147483563)
 WG_KIND_PLAIN, WG_KIND_LOOP, WG_KIND_BATCH_EVEN, WG_KIND_BATCH_ODD = 0, 1, 3, 4
-PRECISIONS = {"fp64": WG_PREC_FP64, "df": WG_PREC_DF}
+PRECISIONS = {"fp64": WG_PREC_FP64, "df": WG_PREC_DF, "dd": WG_PREC_DD}
 PRECISIONS.update({"mod%d" % k: v for k, v in enumerate(WG_PREC_MOD)})
 
 _lock = threading.Lock()
@@ -79,6 +80,10 @@ def build(force=False, verbose=False):
                 raise RuntimeError("nvcc link failed:\n%s\n%s" % (" ".join(cmd), res.stdout.decode()))
             os.replace(tmp, LIB)
         finally:  # no object or half-written library outlives the build, failed or not
+            for _, p in procs:  # compilers still running after an early exit (a Popen that raised)
+                if p.poll() is None:
+                    p.kill()
+                    p.wait()
             for path in objs + [tmp]:
                 if os.path.exists(path):
                     os.unlink(path)

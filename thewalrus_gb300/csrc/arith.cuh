@@ -1,13 +1,16 @@
 // Scalar arithmetic for the sieve kernels.
 //
-// Five scalar types share one interface (struct Ar<S>):
+// Seven scalar types share one interface (struct Ar<S>):
 //   double  real FP64                 c64  complex FP64
 //   dfr     real double-float (FP32)  cdf  complex double-float
+//   ddr     real double-double (FP64) cdd  complex double-double
 //   modp<P> residues modulo a 31-bit prime P in Montgomery form (exact integer sieves)
 // A double-float value is an unevaluated sum hi + lo of two floats (|lo| <= ulp(hi)/2), giving
 // a 48-bit significand from FP32 instructions only.  Products use the FMA error-free
 // transformation (err = fma(a, b, -a*b)); sums use Knuth's two-sum.  Conversions to and from
-// FP64 are exact for the hi part and round the lo part once.
+// FP64 are exact for the hi part and round the lo part once.  A double-double value is the same
+// construction one precision up (two doubles, a 106-bit significand from FP64 instructions), for
+// sums whose terms cancel by more than FP64 can resolve.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -122,6 +125,90 @@ __device__ __forceinline__ dfr df_from_d(double x) {
   return {h, l};
 }
 
+// ---------------------------------------------------------------- double-double primitives
+// The error-free transformations of the double-float type (Knuth's two-sum, Dekker's fast
+// two-sum for |a| >= |b|, the FMA two-product) on doubles.
+struct alignas(16) ddr {
+  double hi, lo;
+};
+struct cdd {
+  ddr re, im;
+};
+__device__ __forceinline__ ddr dd_two_sum(double a, double b) {
+  double s = a + b;
+  double bb = s - a;
+  double e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ ddr dd_fast_two_sum(double a, double b) {
+  double s = a + b;
+  double e = b - (s - a);
+  return {s, e};
+}
+__device__ __forceinline__ ddr dd_add(ddr a, ddr b) {
+  ddr s = dd_two_sum(a.hi, b.hi);
+  double lo = s.lo + (a.lo + b.lo);
+  return dd_fast_two_sum(s.hi, lo);
+}
+__device__ __forceinline__ ddr dd_neg(ddr a) { return {neg_d(a.hi), neg_d(a.lo)}; }
+__device__ __forceinline__ ddr dd_mul(ddr a, ddr b) {
+  double p = a.hi * b.hi;
+  double e = ::fma(a.hi, b.hi, -p);
+  e = ::fma(a.hi, b.lo, e);
+  e = ::fma(a.lo, b.hi, e);
+  return dd_fast_two_sum(p, e);
+}
+__device__ __forceinline__ ddr dd_mul_d(ddr a, double s) {
+  double p = a.hi * s;
+  double e = ::fma(a.hi, s, -p);
+  e = ::fma(a.lo, s, e);
+  return dd_fast_two_sum(p, e);
+}
+// c + a*b with one renormalisation
+__device__ __forceinline__ ddr dd_fma(ddr a, ddr b, ddr c) {
+  double p = a.hi * b.hi;
+  double e = ::fma(a.hi, b.hi, -p);
+  e = ::fma(a.hi, b.lo, e);
+  e = ::fma(a.lo, b.hi, e);
+  ddr s = dd_two_sum(c.hi, p);
+  double lo = s.lo + (c.lo + e);
+  return dd_fast_two_sum(s.hi, lo);
+}
+// c + a*b + d*f  (two products accumulated before one renormalisation)
+__device__ __forceinline__ ddr dd_fma2(ddr a, ddr b, ddr d, ddr f, ddr c) {
+  double p1 = a.hi * b.hi;
+  double e1 = ::fma(a.hi, b.hi, -p1);
+  e1 = ::fma(a.hi, b.lo, e1);
+  e1 = ::fma(a.lo, b.hi, e1);
+  double p2 = d.hi * f.hi;
+  double e2 = ::fma(d.hi, f.hi, -p2);
+  e2 = ::fma(d.hi, f.lo, e2);
+  e2 = ::fma(d.lo, f.hi, e2);
+  ddr s1 = dd_two_sum(c.hi, p1);
+  ddr s2 = dd_two_sum(s1.hi, p2);
+  double lo = (s1.lo + s2.lo) + (c.lo + (e1 + e2));
+  return dd_fast_two_sum(s2.hi, lo);
+}
+// 1/a: the FP64 reciprocal of the high part, then one Newton step r + r (1 - a r) with the
+// residual 1 - a r formed exactly enough (1 - hi(a r) is exact near 1) -- relative error ~2^-104
+__device__ __forceinline__ ddr dd_recip(ddr a) {
+  const double r = recip_newton(a.hi);
+  const ddr t = dd_mul_d(a, r);
+  const double e = (1.0 - t.hi) - t.lo;
+  return dd_fast_two_sum(r, r * e);
+}
+// a / k for a small positive integer k: a times the double-double reciprocal of k
+__device__ __forceinline__ ddr dd_div_int(ddr a, int k) {
+  const double r = 1.0 / (double)k;
+  const ddr rk = {r, ::fma(-(double)k, r, 1.0) * r};
+  return dd_mul(a, rk);
+}
+// deflation threshold of double-double keys (magnitude bits of the high part): k * 2^-92
+__device__ __forceinline__ unsigned long long key_shift_dd(unsigned long long k) {
+  constexpr unsigned long long sh = 92ull << 52;
+  return k > sh ? k - sh : 0ull;
+}
+
 // ---------------------------------------------------------------- traits
 template <class S>
 struct Ar;
@@ -134,6 +221,7 @@ struct Ar<double> {
   static constexpr bool cplx = false;
   static constexpr bool fp64 = true;
   static constexpr bool modular = false;
+  static constexpr bool dd = false;
   __device__ static __forceinline__ S zero() { return 0.0; }
   __device__ static __forceinline__ S one() { return 1.0; }
   __device__ static __forceinline__ S add(S a, S b) { return a + b; }
@@ -167,6 +255,7 @@ struct Ar<c64> {
   static constexpr bool cplx = true;
   static constexpr bool fp64 = true;
   static constexpr bool modular = false;
+  static constexpr bool dd = false;
   __device__ static __forceinline__ S zero() { return {0.0, 0.0}; }
   __device__ static __forceinline__ S one() { return {1.0, 0.0}; }
   __device__ static __forceinline__ S add(S a, S b) { return {a.re + b.re, a.im + b.im}; }
@@ -218,6 +307,7 @@ struct Ar<dfr> {
   static constexpr bool cplx = false;
   static constexpr bool fp64 = false;
   static constexpr bool modular = false;
+  static constexpr bool dd = false;
   __device__ static __forceinline__ S zero() { return {0.f, 0.f}; }
   __device__ static __forceinline__ S one() { return {1.f, 0.f}; }
   __device__ static __forceinline__ S add(S a, S b) { return df_add(a, b); }
@@ -254,6 +344,7 @@ struct Ar<cdf> {
   static constexpr bool cplx = true;
   static constexpr bool fp64 = false;
   static constexpr bool modular = false;
+  static constexpr bool dd = false;
   __device__ static __forceinline__ S zero() { return {{0.f, 0.f}, {0.f, 0.f}}; }
   __device__ static __forceinline__ S one() { return {{1.f, 0.f}, {0.f, 0.f}}; }
   __device__ static __forceinline__ S add(S a, S b) { return {df_add(a.re, b.re), df_add(a.im, b.im)}; }
@@ -302,6 +393,102 @@ struct Ar<cdf> {
   }
 };
 
+// Double-double: FP64's exponent range, so the normalised (unit-subdiagonal) elimination of the
+// FP64 types applies; pivot keys from the high parts.
+template <>
+struct Ar<ddr> {
+  using S = ddr;
+  using Comp = ddr;
+  static constexpr int NC = 1;
+  static constexpr bool cplx = false;
+  static constexpr bool fp64 = true;
+  static constexpr bool modular = false;
+  static constexpr bool dd = true;
+  __device__ static __forceinline__ S zero() { return {0.0, 0.0}; }
+  __device__ static __forceinline__ S one() { return {1.0, 0.0}; }
+  __device__ static __forceinline__ S add(S a, S b) { return dd_add(a, b); }
+  __device__ static __forceinline__ S sub(S a, S b) { return dd_add(a, dd_neg(b)); }
+  __device__ static __forceinline__ S mul(S a, S b) { return dd_mul(a, b); }
+  __device__ static __forceinline__ S fma(S a, S b, S c) { return dd_fma(a, b, c); }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) { return dd_fma(dd_neg(a), b, c); }
+  __device__ static __forceinline__ S neg(S a) { return dd_neg(a); }
+  __device__ static __forceinline__ S conj(S a) { return a; }
+  __device__ static __forceinline__ S scale(S a, double s) { return dd_mul_d(a, s); }
+  __device__ static __forceinline__ S div_int(S a, int k) { return dd_div_int(a, k); }
+  __device__ static __forceinline__ S from_c64(c64 v) { return {v.re, 0.0}; }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {a.hi, 0.0}; }
+  __device__ static __forceinline__ c64 lo_c64(S a) { return {a.lo, 0.0}; }
+  __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a.hi); }
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_dd(k); }
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
+  __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a.hi) == 0; }
+  __device__ static __forceinline__ S recip(S a) { return dd_recip(a); }
+  __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
+  __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) { a = v; }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return dd_add(a, b); }
+  __device__ static __forceinline__ Comp shfl_xor(Comp v, int m) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+  }
+  __device__ static __forceinline__ S shfl(S v, int src) {
+    return {__shfl_sync(0xffffffffu, v.hi, src), __shfl_sync(0xffffffffu, v.lo, src)};
+  }
+};
+
+template <>
+struct Ar<cdd> {
+  using S = cdd;
+  using Comp = ddr;
+  static constexpr int NC = 2;
+  static constexpr bool cplx = true;
+  static constexpr bool fp64 = true;
+  static constexpr bool modular = false;
+  static constexpr bool dd = true;
+  __device__ static __forceinline__ S zero() { return {{0.0, 0.0}, {0.0, 0.0}}; }
+  __device__ static __forceinline__ S one() { return {{1.0, 0.0}, {0.0, 0.0}}; }
+  __device__ static __forceinline__ S add(S a, S b) { return {dd_add(a.re, b.re), dd_add(a.im, b.im)}; }
+  __device__ static __forceinline__ S sub(S a, S b) { return {dd_add(a.re, dd_neg(b.re)), dd_add(a.im, dd_neg(b.im))}; }
+  __device__ static __forceinline__ S mul(S a, S b) {
+    const ddr z = {0.0, 0.0};
+    return {dd_fma2(a.re, b.re, dd_neg(a.im), b.im, z), dd_fma2(a.re, b.im, a.im, b.re, z)};
+  }
+  __device__ static __forceinline__ S fma(S a, S b, S c) {
+    return {dd_fma2(a.re, b.re, dd_neg(a.im), b.im, c.re), dd_fma2(a.re, b.im, a.im, b.re, c.im)};
+  }
+  __device__ static __forceinline__ S fnma(S a, S b, S c) {
+    return {dd_fma2(dd_neg(a.re), b.re, a.im, b.im, c.re), dd_fma2(dd_neg(a.re), b.im, dd_neg(a.im), b.re, c.im)};
+  }
+  __device__ static __forceinline__ S neg(S a) { return {dd_neg(a.re), dd_neg(a.im)}; }
+  __device__ static __forceinline__ S conj(S a) { return {a.re, dd_neg(a.im)}; }
+  __device__ static __forceinline__ S scale(S a, double s) { return {dd_mul_d(a.re, s), dd_mul_d(a.im, s)}; }
+  __device__ static __forceinline__ S div_int(S a, int k) { return {dd_div_int(a.re, k), dd_div_int(a.im, k)}; }
+  __device__ static __forceinline__ S from_c64(c64 v) { return {{v.re, 0.0}, {v.im, 0.0}}; }
+  __device__ static __forceinline__ c64 to_c64(S a) { return {a.re.hi, a.im.hi}; }
+  __device__ static __forceinline__ c64 lo_c64(S a) { return {a.re.lo, a.im.lo}; }
+  __device__ static __forceinline__ unsigned long long key(S a) {
+    const unsigned long long x = absbits_d(a.re.hi), y = absbits_d(a.im.hi);
+    return x > y ? x : y;
+  }
+  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_dd(k); }
+  __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
+  __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re.hi) | absbits_d(a.im.hi)) == 0; }
+  __device__ static __forceinline__ S recip(S a) {
+    const ddr z = {0.0, 0.0};
+    const ddr d = dd_recip(dd_fma2(a.re, a.re, a.im, a.im, z));
+    return {dd_mul(a.re, d), dd_neg(dd_mul(a.im, d))};
+  }
+  __device__ static __forceinline__ Comp comp(const S& a, int i) { return i ? a.im : a.re; }
+  __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) {
+    if (i) a.im = v; else a.re = v;
+  }
+  __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return dd_add(a, b); }
+  __device__ static __forceinline__ Comp shfl_xor(Comp v, int m) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, m), __shfl_xor_sync(0xffffffffu, v.lo, m)};
+  }
+  __device__ static __forceinline__ S shfl(S v, int src) {
+    return {{__shfl_sync(0xffffffffu, v.re.hi, src), __shfl_sync(0xffffffffu, v.re.lo, src)},
+            {__shfl_sync(0xffffffffu, v.im.hi, src), __shfl_sync(0xffffffffu, v.im.lo, src)}};
+  }
+};
 
 // ---------------------------------------------------------------- residues modulo a prime
 // Exact arithmetic for integer inputs: every step of the sieve (elimination with any nonzero
@@ -343,6 +530,7 @@ struct Ar<modp<P>> {
   static constexpr bool cplx = false;
   static constexpr bool fp64 = true;  // exact zero tests, normalised (unit-subdiagonal) elimination
   static constexpr bool modular = true;
+  static constexpr bool dd = false;
   __device__ static __forceinline__ S zero() { return S{0u}; }
   __device__ static __forceinline__ S one() { return S{M::R1}; }
   __device__ static __forceinline__ S add(S a, S b) {

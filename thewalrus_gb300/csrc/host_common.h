@@ -3,6 +3,7 @@
 // schedules.
 #pragma once
 #include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "kernels.h"
@@ -17,10 +18,12 @@ static inline cudaError_t sieve_tables_all(const double* binom, const double* in
 
 // scalar classes
 enum SType { ST_REAL64 = 0, ST_CPLX64 = 1, ST_REALDF = 2, ST_CPLXDF = 3, ST_MOD0 = 4, ST_MOD1 = 5, ST_MOD2 = 6,
-             ST_MOD3 = 7, ST_MOD4 = 8 };
-static inline bool stype_mod(int st) { return st >= ST_MOD0; }
+             ST_MOD3 = 7, ST_MOD4 = 8, ST_REALDD = 9, ST_CPLXDD = 10 };
+static inline bool stype_mod(int st) { return st >= ST_MOD0 && st <= ST_MOD4; }
+static inline bool stype_dd(int st) { return st == ST_REALDD || st == ST_CPLXDD; }
 static size_t stype_bytes(int st) {
   if (stype_mod(st)) return 4;
+  if (stype_dd(st)) return st == ST_REALDD ? 16 : 32;
   return (st == ST_REAL64 || st == ST_REALDF) ? 8 : 16;
 }
 static const uint32_t MOD_PRIMES[5] = {2147483647u, 2147483629u, 2147483587u, 2147483579u, 2147483563u};
@@ -41,6 +44,8 @@ static inline cudaError_t sieve_launch(int stype, const SieveParams& p, int ctas
     case ST_MOD1: return sieve_launch_mod1(p, ctas, wpc, st);
     case ST_MOD2: return sieve_launch_mod2(p, ctas, wpc, st);
     case ST_MOD3: return sieve_launch_mod3(p, ctas, wpc, st);
+    case ST_REALDD: return sieve_launch_fdd(p, ctas, wpc, st);
+    case ST_CPLXDD: return sieve_launch_cdd(p, ctas, wpc, st);
     default: return sieve_launch_mod4(p, ctas, wpc, st);
   }
 }
@@ -55,6 +60,8 @@ static inline int sieve_occupancy(int stype, int wpc, int smem) {
     case ST_MOD1: return sieve_occupancy_mod1(wpc, smem);
     case ST_MOD2: return sieve_occupancy_mod2(wpc, smem);
     case ST_MOD3: return sieve_occupancy_mod3(wpc, smem);
+    case ST_REALDD: return sieve_occupancy_fdd(wpc, smem);
+    case ST_CPLXDD: return sieve_occupancy_cdd(wpc, smem);
     default: return sieve_occupancy_mod4(wpc, smem);
   }
 }
@@ -69,7 +76,25 @@ static inline cudaError_t sieve_tables_all(const double* binom, const double* in
   if (e == cudaSuccess) e = sieve_tables_mod2(binom, inv);
   if (e == cudaSuccess) e = sieve_tables_mod3(binom, inv);
   if (e == cudaSuccess) e = sieve_tables_mod4(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_fdd(binom, inv);
+  if (e == cudaSuccess) e = sieve_tables_cdd(binom, inv);
   return e;
+}
+
+// Launch shape for a per-warp workspace of `bytes`: warps per CTA (at most wpc_cap) for the most
+// resident warps per SM -- shared memory and registers decide how many CTAs fit -- larger CTAs
+// on ties, e.g. 2 CTAs x 7 warps where 1 x 8 would leave room unused.  Returns {wpc, CTAs per
+// SM}; wpc 0 when not even one warp fits.
+static inline std::pair<int, int> best_shape(int stype, int bytes, int wpc_cap) {
+  const int max_smem = 227 * 1024;
+  const int wmax = std::min(wpc_cap, max_smem / bytes);
+  if (wmax < 1) return {0, 0};
+  int wpc = wmax, per_sm = sieve_occupancy(stype, wmax, wmax * bytes);
+  for (int w = wmax - 1; w >= std::max(1, wmax / 2); --w) {
+    const int ps = sieve_occupancy(stype, w, w * bytes);
+    if (ps * w > per_sm * wpc) { wpc = w; per_sm = ps; }
+  }
+  return {wpc, per_sm};
 }
 
 // tilewin: La Budde's coefficient rows live in dead tile columns (only rows 0..2 need `win`)

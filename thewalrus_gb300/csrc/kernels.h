@@ -1,6 +1,6 @@
 // Sieve-kernel instantiations live in one translation unit per scalar class (kernels_c64.cu,
-// kernels_cdf.cu, kernels_f64.cu, kernels_fdf.cu, kernels_mod{0..4}.cu: residues modulo one
-// prime each) so that they compile in parallel.  Each unit
+// kernels_cdf.cu, kernels_f64.cu, kernels_fdf.cu, kernels_cdd.cu, kernels_fdd.cu,
+// kernels_mod{0..4}.cu: residues modulo one prime each) so that they compile in parallel.  Each unit
 // instantiates sieve_kernel<S> and holds its own copy of the constant tables (binomials,
 // reciprocals), which the host fills through sieve_tables_*.
 #pragma once
@@ -19,6 +19,8 @@ WG_KERNEL_UNIT_DECL(c64)
 WG_KERNEL_UNIT_DECL(cdf)
 WG_KERNEL_UNIT_DECL(f64)
 WG_KERNEL_UNIT_DECL(fdf)
+WG_KERNEL_UNIT_DECL(cdd)
+WG_KERNEL_UNIT_DECL(fdd)
 WG_KERNEL_UNIT_DECL(mod0)
 WG_KERNEL_UNIT_DECL(mod1)
 WG_KERNEL_UNIT_DECL(mod2)

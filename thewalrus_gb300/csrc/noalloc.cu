@@ -132,8 +132,11 @@ static __global__ void noalloc_setup_kernel(unsigned char* scratch, const InstDe
     ChunkDev ch;
     ch.inst = 0;
     ch.part = c;
-    ch.t0 = inst.steps * c / nchunks;
-    ch.t1 = inst.steps * (c + 1) / nchunks;
+    // chunk c = [q c + min(c, r), q (c+1) + min(c+1, r)) with steps = q nchunks + r: no product
+    // exceeds steps, so nothing overflows for any accepted term count
+    const long long q = inst.steps / nchunks, r = inst.steps % nchunks;
+    ch.t0 = q * c + (c < r ? c : r);
+    ch.t1 = q * (c + 1) + (c + 1 < r ? c + 1 : r);
     reinterpret_cast<ChunkDev*>(scratch + kOffChunks)[c] = ch;
   }
 }
@@ -191,15 +194,17 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   d.nchunks = 0;  // set below
   const int st = dtype == WG_COMPLEX128 ? ST_CPLX64 : ST_REAL64;
   const int m_max = 2 * nnz;
+  if (sumr == 0) return err(WG_EINVAL, "no photons (every edge repetition is 0): the hafnian is 1, no sieve to run");
   if (d.K > 250) return err(WG_EINVAL, "size beyond the maximum: photon number above 250");
   if (!tile_rows_ok(st, m_max)) return err(WG_EINVAL, "size beyond the maximum: term matrix too large");
   bool all_odd = d.glynn != 0;
   for (int i = 0; i < E; ++i) all_odd = all_odd && (edge_reps[i] % 2 == 1);
   const WarpLayout L = make_layout(st, m_max, m_max, std::min(d.K, m_max), d.K + 2, 2,
                                    all_odd && d.K < m_max);
-  const int wpc = std::min(8, (227 * 1024) / L.bytes);
+  // the same launch shape as wg_hafnian's for this workspace
+  const std::pair<int, int> sh = best_shape(st, L.bytes, 8);
+  const int wpc = sh.first, per_sm = sh.second;
   if (wpc < 1) return err(WG_EINVAL, "size beyond the maximum: per-warp workspace does not fit");
-  const int per_sm = sieve_occupancy(st, wpc, wpc * L.bytes);
   if (per_sm < 1) return err(WG_ECUDA, "sieve kernel cannot be resident");
   const long long resident = (long long)ds->sms * per_sm * wpc;
   long long nch = std::min<long long>(steps, 4 * resident);

@@ -200,6 +200,16 @@ static inline void put_scalar(unsigned char* dst, int st, double re, double im) 
       memcpy(dst, &h, 4); memcpy(dst + 4, &l, 4);
       break;
     }
+    case ST_REALDD: {  // the input double is the high part exactly
+      const double z = 0.0;
+      memcpy(dst, &re, 8); memcpy(dst + 8, &z, 8);
+      break;
+    }
+    case ST_CPLXDD: {
+      const double z = 0.0;
+      memcpy(dst, &re, 8); memcpy(dst + 8, &z, 8); memcpy(dst + 16, &im, 8); memcpy(dst + 24, &z, 8);
+      break;
+    }
     default: {
       float h = (float)re, l = (float)(re - (double)h);
       float hi = (float)im, li = (float)(im - (double)hi);
@@ -390,7 +400,9 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
     if (maxr > 50) return fail(WG_EINVAL, "exact precision supports edge repetitions up to 50");
     P.stype = ST_MOD0 + (precision - WG_PREC_MOD0);
   } else {
-    P.stype = precision == WG_PREC_DF ? (cplx ? ST_CPLXDF : ST_REALDF) : (cplx ? ST_CPLX64 : ST_REAL64);
+    P.stype = precision == WG_PREC_DF   ? (cplx ? ST_CPLXDF : ST_REALDF)
+              : precision == WG_PREC_DD ? (cplx ? ST_CPLXDD : ST_REALDD)
+                                        : (cplx ? ST_CPLX64 : ST_REAL64);
   }
   // extended matrix [[A, D], [D^T, 0], [oddV, 0], [oddV0, 0]]  ((n+3) x (n+1))
   const int n = in.n, lda = n + 1;
@@ -556,7 +568,7 @@ static int prepare_request(const wg_request& r, const wg_state& st, int precisio
 
 static int build_plan(const wg_instance* v, int count, int precision, const wg_plan_options& opt, wg_plan* pl) {
   if (count < 0 || (count > 0 && !v)) return fail(WG_EINVAL, "bad instance list");
-  if (precision != WG_PREC_FP64 && precision != WG_PREC_DF && !prec_mod(precision))
+  if (precision != WG_PREC_FP64 && precision != WG_PREC_DF && precision != WG_PREC_DD && !prec_mod(precision))
     return fail(WG_EINVAL, "unknown precision %d", precision);
   std::vector<Prepared> P(count);
   for (int i = 0; i < count; ++i) {
@@ -585,27 +597,13 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
     scales.insert(scales.end(), P[i].scales.begin(), P[i].scales.end());
   }
   pl->total_out = out;
-  // launch shape for a per-warp workspace: warps per CTA for the most resident warps per SM
-  // (shared memory and registers decide how many CTAs fit), larger CTAs on ties -- e.g. 2 CTAs x
-  // 7 warps where 1 x 8 would leave room unused.  {wpc, CTAs per SM}; wpc 0 when none fits.
-  const int max_smem = 227 * 1024;
+  // launch shape per (scalar class, per-warp workspace), see best_shape
   std::map<std::pair<int, int>, std::pair<int, int>> shape_memo;
   auto shape = [&](int st, int bytes) -> std::pair<int, int> {
     const auto key = std::make_pair(st, bytes);
     const auto it = shape_memo.find(key);
     if (it != shape_memo.end()) return it->second;
-    const int wmax = std::min(wpc_cap, max_smem / bytes);
-    std::pair<int, int> r{0, 0};
-    if (wmax >= 1) {
-      int wpc = wmax, per_sm = sieve_occupancy(st, wmax, wmax * bytes);
-      for (int w = wmax - 1; w >= std::max(1, wmax / 2); --w) {
-        const int ps = sieve_occupancy(st, w, w * bytes);
-        if (ps * w > per_sm * wpc) { wpc = w; per_sm = ps; }
-      }
-      r = {wpc, per_sm};
-    }
-    shape_memo[key] = r;
-    return r;
+    return shape_memo[key] = best_shape(st, bytes, wpc_cap);
   };
   // groups by (stype, resident warps per SM of the instance's own workspace), so that a small
   // instance does not run at the occupancy of a larger one's workspace; with merge_classes one
@@ -657,9 +655,9 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
         total_cost += P[i].term_cost * (double)(P[i].t_hi - P[i].t_lo);
       }
     G.L = make_layout(G.stype, rows, mb, kc, nser, narr, tile);
-    if (max_smem / G.L.bytes < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
     const auto sh = shape(G.stype, G.L.bytes);
     const int wpc = sh.first, per_sm = sh.second;
+    if (wpc < 1) return fail(WG_EINVAL, "per-warp workspace of %d bytes does not fit", G.L.bytes);
     if (per_sm < 1) {
       cudaGetLastError();
       return fail(WG_ECUDA, "sieve kernel cannot be resident (workspace %d B x %d warps)", G.L.bytes, wpc);
@@ -684,6 +682,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
       const double tc = P[i].term_cost;
       const long long hi = P[i].t_hi, pmin = std::max(1LL, (long long)std::ceil(min_cost / tc));
       d.part_base = nparts;
+      d.pstride = stype_dd(P[i].stype) ? 2 * d.nout : d.nout;  // dd: sums and compensations
       int nch = 0;
       for (long long t = P[i].t_lo; t < hi; ++nch) {
         const double want = std::min(remaining / div, kMaxChunkCost * chunk_scale);
@@ -691,7 +690,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
         per = std::min(per, hi - t);
         ChunkDev ch;
         ch.inst = i;
-        ch.part = nparts + nch * d.nout;
+        ch.part = nparts + nch * d.pstride;
         ch.t0 = t;
         ch.t1 = t + per;
         pl->chunks.push_back(ch);
@@ -699,7 +698,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
         t += per;
       }
       d.nchunks = nch;
-      nparts += nch * d.nout;
+      nparts += nch * d.pstride;
     }
     G.chunk_count = (int)pl->chunks.size() - G.chunk_begin;
     G.ctas = (int)std::min<long long>((long long)g_num_sms * per_sm, (G.chunk_count + wpc - 1) / wpc);

@@ -52,7 +52,9 @@ struct InstDev {
   c64 oddloop, oddloop0;
   // reduction bookkeeping
   int part_base;   // first partial slot of this instance
-  int nchunks;     // chunks of this instance (partials are [part_base, part_base + nchunks*nout))
+  int nchunks;     // chunks of this instance (partials are [part_base, part_base + nchunks*pstride))
+  int pstride;     // partial slots per chunk: nout, or 2 nout (sums, then compensations) for
+                   // double-double kinds; 0 reads as nout
   int out_base;    // first output slot
   int scale_base;  // first output scale
 };
@@ -165,6 +167,9 @@ __device__ __forceinline__ S warp_sum(S v) {
 
 __device__ __forceinline__ double shfl_up_c(double v, int off) { return __shfl_up_sync(0xffffffffu, v, off); }
 __device__ __forceinline__ dfr shfl_up_c(dfr v, int off) {
+  return {__shfl_up_sync(0xffffffffu, v.hi, off), __shfl_up_sync(0xffffffffu, v.lo, off)};
+}
+__device__ __forceinline__ ddr shfl_up_c(ddr v, int off) {
   return {__shfl_up_sync(0xffffffffu, v.hi, off), __shfl_up_sync(0xffffffffu, v.lo, off)};
 }
 template <uint32_t P>
@@ -638,7 +643,11 @@ __device__ void inv_sqrt_series(const S* __restrict__ cpoly, int Kc, S* __restri
         if (n == k + 1) acc = A::neg(A::mul(acc, inv_of<S>(n)));
       } else {
         acc = A::fma(cpoly[n - k], A::scale(gk, 0.5 * (double)(n + k)), g[n]);
-        if (n == k + 1) acc = A::scale(acc, -inv_int(n));
+        if constexpr (A::dd) {  // 1/n to the type's precision
+          if (n == k + 1) acc = A::neg(A::div_int(acc, n));
+        } else {
+          if (n == k + 1) acc = A::scale(acc, -inv_int(n));
+        }
       }
       g[n] = acc;
     }
@@ -664,7 +673,11 @@ __device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, in
         if (n == k + 1) acc = A::mul(acc, inv_of<S>(n));
       } else {
         acc = A::fma(A::scale(q[n - k], (double)(n - k)), ek, e[n]);
-        if (n == k + 1) acc = A::scale(acc, inv_int(n));
+        if constexpr (A::dd) {
+          if (n == k + 1) acc = A::div_int(acc, n);
+        } else {
+          if (n == k + 1) acc = A::scale(acc, inv_int(n));
+        }
       }
       e[n] = acc;
     }
@@ -858,8 +871,14 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
           if (parity) pre = -pre;
           if (halve) pre *= 0.5;
           const c64 z = A::to_c64(f);
-          neumaier(s_re, k_re, pre * z.re);
-          neumaier(s_im, k_im, pre * z.im);
+          const double xr = pre * z.re, xi = pre * z.im;
+          neumaier(s_re, k_re, xr);
+          neumaier(s_im, k_im, xi);
+          if constexpr (A::dd) {  // the product's rounding error and the low parts join the compensation
+            const c64 zl = A::lo_c64(f);
+            k_re += ::fma(pre, z.re, -xr) + pre * zl.re;
+            k_im += ::fma(pre, z.im, -xi) + pre * zl.im;
+          }
         }
       };
       const int g0 = __shfl_sync(0xffffffffu, g, 0);
@@ -990,6 +1009,11 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
     }
     if constexpr (A::modular) {
       if (lane < nout) P.partials[ch.part + lane] = make_double2((double)A::to_c64(macc).re, 0.0);
+    } else if constexpr (A::dd) {  // sum and compensation kept apart: 2 nout slots per chunk
+      if (lane < nout) {
+        P.partials[ch.part + lane] = make_double2(s_re, s_im);
+        P.partials[ch.part + nout + lane] = make_double2(k_re, k_im);
+      }
     } else {
       if (lane < nout) P.partials[ch.part + lane] = make_double2(s_re + k_re, s_im + k_im);
     }
@@ -1025,10 +1049,16 @@ static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst
     const InstDev& I = inst[lo];
     const int o = gw - I.out_base;
     double sr = 0, si = 0, cr = 0, ci = 0;
+    const int ps = I.pstride > I.nout ? I.pstride : I.nout;  // slots per chunk
     for (int c = lane; c < I.nchunks; c += 32) {
-      const double2 v = partials[I.part_base + c * I.nout + o];
+      const double2 v = partials[I.part_base + c * ps + o];
       neumaier(sr, cr, v.x);
       neumaier(si, ci, v.y);
+      if (ps > I.nout) {  // double-double kinds: the chunk's compensation
+        const double2 w = partials[I.part_base + c * ps + I.nout + o];
+        cr += w.x;
+        ci += w.y;
+      }
     }
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
