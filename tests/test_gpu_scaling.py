@@ -87,3 +87,23 @@ def test_general_scaling_terms(n, kind, decades):
         m = t ^ (t >> 1)
         want = complex(oracle.haf_term_range(inst.A, inst.reps, m, m + 1, precision="quad")) * scale
         assert rel(g, want) < RTOL, (t, g, want)
+
+
+@pytest.mark.parametrize("n", [20, 24, 28, 32])
+def test_small_entry_gaussian_state_loops(n):
+    """Loop hafnians of a 64-mode Gaussian state's B (entries ~0.1, so every pivot is below 1):
+    in the normalised elimination the subdiagonal candidates shrink by the product of the
+    pivots against the rows above (1e-15 after 22 columns), which a deflation test made in that
+    frame took for rounding residues -- relative errors of 0.03 at n = 20 up to 760 at n = 28
+    before the test moved to the classic frame.  These sums are well conditioned (sum|term| /
+    |sum| ~ 1e2..1e3): 1e-10 against the oracle."""
+    from thewalrus_gb300.serving import GaussianState
+    st = GaussianState.synthetic(modes=64, seed=3)
+    rng = np.random.default_rng(n)
+    modes = np.sort(rng.choice(64, size=n, replace=False))
+    B, gamma = st.B[np.ix_(modes, modes)], st.gamma[modes]
+    want = complex(oracle.hafnian_repeated(B, [1] * n, mu=gamma, loop=True, precision="long"))
+    assert rel(tw.hafnian_repeated(B, [1] * n, mu=gamma, loop=True), want) < RTOL
+    assert rel(tw.hafnian_repeated(B, [1] * n, mu=gamma, loop=True, precision="dd"), want) < RTOL
+    want = complex(oracle.hafnian(B, precision="long"))
+    assert rel(tw.hafnian(B), want) < RTOL

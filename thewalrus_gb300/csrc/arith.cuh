@@ -40,14 +40,11 @@ __device__ __forceinline__ unsigned long long absbits_d(double x) {
 }
 __device__ __forceinline__ unsigned int absbits_f(float x) { return (unsigned)__float_as_int(x) & 0x7fffffffu; }
 
-// Deflation threshold of a pivot column: the key (magnitude bits) of k * 2^-44 for FP64 keys and
-// k * 2^-40 for the FP32 high parts of double-float keys (0 when that leaves the normal range).
-// Subdiagonal candidates at or below it are rounding residues of an exact cancellation (terms
-// whose matrix repeats a row, such as the two ends of the batch edge) and are treated as zero.
-__device__ __forceinline__ unsigned long long key_shift_d(unsigned long long k) {
-  constexpr unsigned long long sh = 44ull << 52;
-  return k > sh ? k - sh : 0ull;
-}
+// Deflation threshold of a pivot column for the double-float keys (FP32 high parts): k * 2^-40,
+// 0 when that leaves the normal range.  Subdiagonal candidates at or below it are rounding
+// residues of an exact cancellation (terms whose matrix repeats a row, such as the two ends of
+// the batch edge) and are treated as zero.  The FP64 and double-double types, whose elimination
+// is normalised, compare in the classic frame instead (hessenberg_elim), at 2^-DEFLATE_BITS.
 __device__ __forceinline__ unsigned long long key_shift_f(unsigned long long k) {
   constexpr unsigned long long sh = 40ull << 23;
   return k > sh ? k - sh : 0ull;
@@ -203,12 +200,6 @@ __device__ __forceinline__ ddr dd_div_int(ddr a, int k) {
   const ddr rk = {r, ::fma(-(double)k, r, 1.0) * r};
   return dd_mul(a, rk);
 }
-// deflation threshold of double-double keys (magnitude bits of the high part): k * 2^-92
-__device__ __forceinline__ unsigned long long key_shift_dd(unsigned long long k) {
-  constexpr unsigned long long sh = 92ull << 52;
-  return k > sh ? k - sh : 0ull;
-}
-
 // ---------------------------------------------------------------- traits
 template <class S>
 struct Ar;
@@ -222,6 +213,7 @@ struct Ar<double> {
   static constexpr bool fp64 = true;
   static constexpr bool modular = false;
   static constexpr bool dd = false;
+  static constexpr int DEFLATE_BITS = 44;  // deflation threshold 2^-44 (normalised elimination)
   __device__ static __forceinline__ S zero() { return 0.0; }
   __device__ static __forceinline__ S one() { return 1.0; }
   __device__ static __forceinline__ S add(S a, S b) { return a + b; }
@@ -235,7 +227,6 @@ struct Ar<double> {
   __device__ static __forceinline__ S from_c64(c64 v) { return v.re; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {a, 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a); }
-  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_d(k); }
   // 32-bit pivot key: sign-free exponent and the top 20 mantissa bits
   __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a) == 0; }
@@ -256,6 +247,7 @@ struct Ar<c64> {
   static constexpr bool fp64 = true;
   static constexpr bool modular = false;
   static constexpr bool dd = false;
+  static constexpr int DEFLATE_BITS = 44;
   __device__ static __forceinline__ S zero() { return {0.0, 0.0}; }
   __device__ static __forceinline__ S one() { return {1.0, 0.0}; }
   __device__ static __forceinline__ S add(S a, S b) { return {a.re + b.re, a.im + b.im}; }
@@ -280,7 +272,6 @@ struct Ar<c64> {
     const unsigned long long x = absbits_d(a.re), y = absbits_d(a.im);
     return x > y ? x : y;
   }
-  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_d(k); }
   // 32-bit pivot key: sign-free exponent and the top 20 mantissa bits
   __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re) | absbits_d(a.im)) == 0; }
@@ -404,6 +395,7 @@ struct Ar<ddr> {
   static constexpr bool fp64 = true;
   static constexpr bool modular = false;
   static constexpr bool dd = true;
+  static constexpr int DEFLATE_BITS = 92;
   __device__ static __forceinline__ S zero() { return {0.0, 0.0}; }
   __device__ static __forceinline__ S one() { return {1.0, 0.0}; }
   __device__ static __forceinline__ S add(S a, S b) { return dd_add(a, b); }
@@ -419,7 +411,6 @@ struct Ar<ddr> {
   __device__ static __forceinline__ c64 to_c64(S a) { return {a.hi, 0.0}; }
   __device__ static __forceinline__ c64 lo_c64(S a) { return {a.lo, 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a.hi); }
-  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_dd(k); }
   __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_d(a.hi) == 0; }
   __device__ static __forceinline__ S recip(S a) { return dd_recip(a); }
@@ -443,6 +434,7 @@ struct Ar<cdd> {
   static constexpr bool fp64 = true;
   static constexpr bool modular = false;
   static constexpr bool dd = true;
+  static constexpr int DEFLATE_BITS = 92;
   __device__ static __forceinline__ S zero() { return {{0.0, 0.0}, {0.0, 0.0}}; }
   __device__ static __forceinline__ S one() { return {{1.0, 0.0}, {0.0, 0.0}}; }
   __device__ static __forceinline__ S add(S a, S b) { return {dd_add(a.re, b.re), dd_add(a.im, b.im)}; }
@@ -468,7 +460,6 @@ struct Ar<cdd> {
     const unsigned long long x = absbits_d(a.re.hi), y = absbits_d(a.im.hi);
     return x > y ? x : y;
   }
-  __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_dd(k); }
   __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)(k >> 32); }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_d(a.re.hi) | absbits_d(a.im.hi)) == 0; }
   __device__ static __forceinline__ S recip(S a) {

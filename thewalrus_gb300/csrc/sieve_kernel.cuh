@@ -309,6 +309,17 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
 
+  // Normalised forms: row i of the tile is the classic elimination's row i divided by d_i, the
+  // pivot row i was divided by when it was reduced (d = 1 for rows never divided), and column j
+  // carries the factor d_j.  So the candidates of column j are d_j x their classic values and an
+  // upper entry (i, j) is d_j / d_i x its classic value: with pivots below 1 (matrices of small
+  // entries, such as Gaussian states' B) the candidates fall geometrically against the upper
+  // rows -- by 1e-15 after 22 columns at |B| ~ 0.1 -- although nothing cancels.  The deflation
+  // test is made in the classic frame: each upper key is raised by log2 d_i of its row, kept per
+  // lane for the lane's rows nb + lane + 32 k (k < 3) as the pivot's binary exponent.
+  constexpr bool kNorm = A::fp64 && !A::modular;
+  int dexp[3] = {0, 0, 0};
+
   for (int j = 0; j + 1 < mb; ++j) {
     // --- pivot: largest max(|re|,|im|) in column j, rows j+1..mb-1, to 13 (FP64) or 16 (FP32
     // high part) significant bits, ties to the lowest row: the key's top bits and 127 - row packed
@@ -318,22 +329,38 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
     // uk does -- one vote, off the reduction.
     unsigned best = 0;
     unsigned long long uk = 0;
-    for (int a = nb + lane; a < mb; a += 32) {
-      const unsigned long long k = A::key(W[a * ldw + j]);
-      if (a > j) {
-        const unsigned pk = (A::key32(k) & ~0x7fu) | (unsigned)(127 - a);
-        best = pk > best ? pk : best;
-      } else {
-        uk = k > uk ? k : uk;
+    long long ukn = 0;  // normalised forms: largest upper key in the classic frame
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      const int a = nb + lane + 32 * q;
+      if (a < mb) {
+        const unsigned long long k = A::key(W[a * ldw + j]);
+        if (a > j) {
+          const unsigned pk = (A::key32(k) & ~0x7fu) | (unsigned)(127 - a);
+          best = pk > best ? pk : best;
+        } else if constexpr (kNorm) {
+          const long long k32 = (long long)A::key32(k);
+          const long long adj = k32 ? k32 + ((long long)dexp[q] << 20) : 0;
+          ukn = adj > ukn ? adj : ukn;
+        } else {
+          uk = k > uk ? k : uk;
+        }
       }
     }
     best = __reduce_max_sync(0xffffffffu, best);
-    if (__any_sync(0xffffffffu, (best & ~0x7fu) <= (A::key32(A::key_deflate(uk)) & ~0x7fu))) {
+    bool deflate;
+    if constexpr (kNorm) {
+      const long long lb = (long long)(best & ~0x7fu);
+      deflate = __any_sync(0xffffffffu, lb == 0 || lb <= ukn - ((long long)A::DEFLATE_BITS << 20));
+    } else {
+      deflate = __any_sync(0xffffffffu, (best & ~0x7fu) <= (A::key32(A::key_deflate(uk)) & ~0x7fu));
+    }
+    if (deflate) {
       // nothing to eliminate: the candidates are zero or rounding residues of an exact
       // cancellation; the subdiagonal becomes an exact zero and the column below it is cleared
       for (int a = j + 1 + lane; a < mb; a += 32) W[a * ldw + j] = A::zero();
       __syncwarp();
-      continue;
+      continue;  // row j+1 is not divided: d_{j+1} = 1
     }
     const int p = 127 - (int)(best & 0x7fu);
     if (p != j + 1) {
@@ -352,6 +379,12 @@ __device__ void hessenberg_elim(S* __restrict__ W, S* __restrict__ xv, int mb, i
     }
     const S piv = W[(j + 1) * ldw + j];
     const S rp = A::recip(piv);
+    if constexpr (kNorm) {  // row j+1 is divided by piv: d_{j+1} = |piv| (as a binary exponent)
+      const int e = (int)(A::key32(A::key(piv)) >> 20) - 1023;
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        if (nb + lane + 32 * q == j + 1) dexp[q] = e;
+    }
     if constexpr (A::fp64) {
       for (int b = j + 1 + lane; b < mb; b += 32) xv[b] = (b == j + 1) ? piv : W[b * ldw + j];
       __syncwarp();
