@@ -257,14 +257,14 @@ def run_gpu(args, rank, world, local):
     flops = costmodel.plain_hafnian_flops(n, complex_input=args.matrix == "complex")
     mean_s = total_ms / args.steps * 1e-3
     achieved = flops / mean_s / 1e12
-    peak = fp64_peak if args.precision == "fp64" else fp32_peak
+    peak = fp32_peak if args.precision == "df" else fp64_peak  # double-double runs on the FP64 pipe
     if rank != 0:
         return
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": (value * PUBLISHED_N40_SECONDS if n == N_MATRIX else None),
-        "dtype": "f64" if args.precision == "fp64" else "df32",
+        "dtype": {"fp64": "f64", "df": "df32", "dd": "dd64"}[args.precision],
         "data": "synthetic",
         "config": {"workload": "hafnian %dx%d %s, seed 0, %d sieve terms"
                                % (n, n, "complex128 (G+G^T)/2" if args.matrix == "complex"
@@ -273,7 +273,7 @@ def run_gpu(args, rank, world, local):
                    "l2": "flushed between steps (256 MiB write, outside the timed events)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
-        "roofline": {"bound": "fp64" if args.precision == "fp64" else "fp32",
+        "roofline": {"bound": "fp32" if args.precision == "df" else "fp64",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
                      "traffic_note": "DRAM bytes need an ncu capture, not taken inside the bench",
@@ -725,7 +725,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_MATRIX, help="matrix size (40 is the benchmark)")
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--precision", choices=["fp64", "df"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "df", "dd"], default="fp64")
     ap.add_argument("--matrix", choices=["complex", "real"], default="complex",
                     help="the n-x-n workload: complex symmetric (the benchmark) or real signed")
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
