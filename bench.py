@@ -373,7 +373,8 @@ def batch_summary(args):
 def serve_summary(args):
     """Serving (Poisson streams of probability requests on four 64-mode Gaussian states, patterns
     of 8-44 photons, at most 2 per mode): p50/p99 latency and hafnians/s at two arrival rates with
-    ``--serve-count`` requests each; the higher rate's requests also one call each (matrices
+    ``--serve-count`` requests each (the same requests, arrival times scaled), admitted cheapest
+    first; the higher rate's requests also admitted oldest first, and one call each (matrices
     formed on the device, one plan per request, synchronous); loop hafnians of the requests with
     at most 24 photons against the long-double oracle."""
     import numpy as np
@@ -404,6 +405,12 @@ def serve_summary(args):
                 lhaf = r["amplitude"] / st.norm(pat)
                 err = max(err, abs(lhaf - want) / abs(want))
                 checked += 1
+    # the same requests at the top rate, admitted oldest first (no cost ordering) for contrast
+    fifo = ProbabilityServer(states, precision="fp64", max_batch=256, streams=3, order="arrival")
+    t0 = time.perf_counter()
+    res = fifo.serve(reqs)
+    arrival = summary(res, makespan=time.perf_counter() - t0)
+    arrival["rate"] = args.serve_rates[-1]
     done = 0
     t0 = time.perf_counter()
     for _, sidx, pat in reqs:
@@ -418,7 +425,9 @@ def serve_summary(args):
     per_call_s = time.perf_counter() - t0
     return {"workload": "%d requests per rate, Poisson arrivals, 4 synthetic 64-mode pure states, 8-44 photons"
                         % args.serve_count,
-            "rates": rows, "per_call": {"requests": done, "seconds": per_call_s, "hafnians_per_s": done / per_call_s,
+            "admission": "cheapest first, batches closed at ~25 ms of GPU work",
+            "rates": rows, "arrival_order_at_top_rate": arrival,
+            "per_call": {"requests": done, "seconds": per_call_s, "hafnians_per_s": done / per_call_s,
                                         "same_requests_as_rate": args.serve_rates[-1]},
             "max_rel_err_vs_oracle_ld": err, "oracle_checked": checked}
 
@@ -597,10 +606,10 @@ def run_precision(args):
 
     * n = 20 (``--precision-n``), ``--precision-seeds`` seeds per class: against the _Float128
       oracle.
-    * n = 48, the large-size table: random 0/1 graphs (edge probability 0.5) and integer
-      non-negative matrices (rint(|G| + |G|^T)) against their exact hafnians (the exact sieve over
-      residues, pinned against the CPU modular oracle), ``--precision-seeds48`` seeds each;
-      signed real and complex matrices against the double-double sieve (pinned against the
+    * n = 48, the large-size table: random 0/1 graphs (edge probability 0.5, ``--precision-seeds48``
+      seeds) and integer non-negative matrices (floor(|G| + |G|^T), entries 0..5; a quarter as
+      many seeds) against their exact hafnians (the exact sieve over residues, pinned against
+      the CPU modular oracle); signed real and complex matrices against the double-double sieve (pinned against the
       _Float128 oracle to 1e-20 at n <= 20), ``--precision-dd-seeds`` seeds (half that for the
       complex class, whose double-double run takes minutes).  Times per hafnian per mode."""
     import numpy as np
@@ -635,7 +644,7 @@ def run_precision(args):
     n = 48
     large = {}
     classes = [("adjacency01", lambda sd: wl.adjacency01(n, seed=sd), "exact", args.precision_seeds48),
-               ("int_nonneg", lambda sd: np.rint(wl.real_nonneg(n, seed=sd)), "exact", args.precision_seeds48 // 4),
+               ("int_nonneg", lambda sd: np.floor(wl.real_nonneg(n, seed=sd)), "exact", args.precision_seeds48 // 4),
                ("real_signed", lambda sd: wl.real_signed(n, seed=sd), "dd", args.precision_dd_seeds),
                ("complex", lambda sd: wl.complex_symmetric(n, seed=sd), "dd", max(1, args.precision_dd_seeds // 2))]
     for name, gen, truth_mode, seeds in classes:

@@ -174,6 +174,15 @@ typedef struct wg_request {
   int32_t oddmode;           /* unpaired mode or -1 */
 } wg_request;
 int wg_state_create(const double* B, const double* gamma, int M, wg_state** state);
+/* The same state formed on the device from a pure Gaussian state's xp-ordered covariance
+ * (2M x 2M, row-major) and means (2M) with the conventions of thewalrus/quantum/conversions.py:
+ * 69-170 and fock_tensors.py:45-98: Husimi Q, B = -(Q^-1)[M:, :M], alpha, gamma = alpha - B
+ * alpha^*.  Q is factored by a Cholesky decomposition on the GPU (a covariance whose Q is not
+ * positive definite is rejected with WG_EINVAL).  vacuum receives <0|psi> = exp(-(|alpha|^2 -
+ * alpha^H B alpha^*)/2) / det(Q)^(1/4); B_out (M x M complex) and gamma_out (M complex), when not
+ * NULL, receive copies of the resident matrices.  M <= 512. */
+int wg_state_create_from_cov(const double* cov, const double* mu, int M, double hbar, wg_state** state,
+                             double vacuum[2], double* B_out, double* gamma_out);
 int wg_state_destroy(wg_state* state);
 int wg_plan_create_requests(const wg_state* state, const wg_request* req, int count, int precision,
                             const wg_plan_options* options, wg_plan** plan);

@@ -51,3 +51,31 @@ def test_admission_respects_memory_budget():
     srv = ProbabilityServer(states, max_batch=64, streams=2, mem_budget=tight)
     res = srv.serve(reqs)
     assert len({r["batch"] for r in res}) == len(reqs)
+
+
+def test_state_formed_on_the_device_from_the_covariance(golden):
+    """wg_state_create_from_cov: the Husimi matrix, its Cholesky factor, B, gamma and the vacuum
+    amplitude formed on the GPU from the covariance equal the host conversions, and the served
+    amplitudes equal the reference's pure_state_amplitude values."""
+    pytest.importorskip("torch")
+    cases = golden["pure"]
+    host = GaussianState.from_cov(cases[0]["mu"], cases[0]["cov"])
+    dev = GaussianState.from_cov_on_device(cases[0]["mu"], cases[0]["cov"])
+    assert np.max(np.abs(dev.B - host.B)) <= 1e-13 * np.max(np.abs(host.B))
+    assert np.max(np.abs(dev.gamma - host.gamma)) <= 1e-13 * np.max(np.abs(host.gamma))
+    assert abs(dev.vacuum - host.vacuum) <= 1e-13 * abs(host.vacuum)
+    srv = ProbabilityServer([dev], max_batch=4, streams=2)
+    res = srv.serve([(0.0, 0, np.asarray(c["pattern"])) for c in cases])
+    for c, r in zip(cases, res):
+        ref = complex(c["out"])
+        assert abs(r["amplitude"] - ref) <= RTOL * abs(ref) + 1e-15
+    # a larger synthetic state (64 modes, hbar = 1): the device conversion against the host one
+    from thewalrus_gb300 import workloads as wl
+    cov, mu = wl.gaussian_state_cov(64, seed=5, transmission=1.0, disp=0.2)
+    host = GaussianState.from_cov(mu, cov * 0.5, hbar=1)
+    dev = GaussianState.from_cov_on_device(mu, cov * 0.5, hbar=1)
+    assert np.max(np.abs(dev.B - host.B)) <= 1e-12 * np.max(np.abs(host.B))
+    assert abs(dev.vacuum - host.vacuum) <= 1e-12 * abs(host.vacuum)
+    # a covariance whose Husimi matrix is not positive definite (negative variances) is refused
+    with pytest.raises(RuntimeError):
+        GaussianState.from_cov_on_device(np.zeros(8), -2.0 * np.eye(8))

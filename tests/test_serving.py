@@ -31,3 +31,20 @@ def test_poisson_requests_shape():
     res = [{"latency": 0.1 * i, "done": 1.0 + i, "arrival": float(i), "batch": i % 3} for i in range(10)]
     sm = summary(res)
     assert sm["requests"] == 10 and sm["batches"] == 3 and sm["p99_s"] >= sm["p50_s"]
+
+
+def test_request_cost_counts_the_sieve_terms():
+    from thewalrus_gb300._hafnian import matched_reps
+    from thewalrus_gb300.serving import ProbabilityServer
+    for k in (2, 5, 9):
+        pat = np.zeros(30, dtype=np.int64)
+        pat[: 2 * k] = 1
+        # k edges of multiplicity 1: 2^(k-1) terms (the first radix halved), m = 2k, bordered m + 1
+        assert ProbabilityServer.request_cost(matched_reps(pat)) == 2 ** (k - 1) * float(2 * k + 2) ** 3
+    # an unpaired mode: no halving of the first radix
+    pat = np.zeros(10, dtype=np.int64)
+    pat[:3] = 1
+    x, reps, odd = matched_reps(pat)
+    assert odd is not None and ProbabilityServer.request_cost((x, reps, odd)) == 2.0 * 4.0 ** 3
+    costs = [ProbabilityServer.request_cost(matched_reps(np.array([1] * n + [0] * (40 - n)))) for n in (8, 16, 24, 32)]
+    assert costs == sorted(costs)

@@ -13,7 +13,8 @@ Same names, arguments, return conventions and errors as the reference's public f
 
 The host keeps validation, the closed forms for tiny matrices, edge pairing and reordering;
 every sieve runs on the GPU (no CPU fallback).  Extra keyword ``precision`` selects "fp64"
-(default) or "df" (FP32 double-float term arithmetic).  Sieve results come back as
+(default), "df" (FP32 double-float term arithmetic), "dd" (FP64 double-double terms, for sums
+that cancel beyond FP64's reach) or "exact" (integer inputs).  Sieve results come back as
 ``numpy.complex128`` also for real input, as in the reference.
 """
 import numpy as np
@@ -308,7 +309,9 @@ def hafnian(A, loop=False, rtol=1e-05, atol=1e-08, approx=False, num_samples=100
     Args and results as ``thewalrus.hafnian``; ``method`` is "glynn" or "inclexcl" (the loop
     hafnian always uses the finite-difference sieve, as in the reference).  ``precision``:
     None (exact for integer-valued real inputs, FP64 otherwise), "fp64", "df" (double-float
-    terms) or "exact" (integer inputs only).
+    terms), "dd" (double-double terms: ~14x the FP64 time, for sieve sums whose terms cancel by
+    more than ~1e6, e.g. the loop hafnians of many-photon Gaussian-state patterns) or "exact"
+    (integer inputs only).
     """
     input_validation(A, rtol=rtol, atol=atol)
     glynn = _method_glynn(method) if not loop else True

@@ -18,7 +18,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 SOURCES = ["sieve.cu", "noalloc.cu", "kernels_c64.cu", "kernels_cdf.cu", "kernels_f64.cu", "kernels_fdf.cu",
            "kernels_cdd.cu", "kernels_fdd.cu", "kernels_mod0.cu", "kernels_mod1.cu", "kernels_mod2.cu",
            "kernels_mod3.cu", "kernels_mod4.cu"]
-DEPS = SOURCES + ["sieve_kernel.cuh", "arith.cuh", "host_common.h", "kernels.h", "kernels_unit.cuh"]
+DEPS = SOURCES + ["sieve_kernel.cuh", "arith.cuh", "host_common.h", "kernels.h", "kernels_unit.cuh",
+                  "state_glue.cuh"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-shared"]
 
@@ -118,7 +119,7 @@ EXPORTS = [
     "wg_plan_kernel_launches", "wg_plan_partials", "wg_plan_chunk", "wg_plan_transfer_bytes",
     "wg_plan_destroy", "wg_run",
     "wg_measure_fp_peaks", "wg_hafnian_noalloc", "wg_state_create", "wg_state_destroy",
-    "wg_plan_create_requests", "wg_plan_device_bytes", "wg_instance_terms",
+    "wg_plan_create_requests", "wg_plan_device_bytes", "wg_instance_terms", "wg_state_create_from_cov",
 ]
 
 
@@ -170,6 +171,7 @@ def load(build_if_needed=True):
     lib.wg_measure_fp_peaks.argtypes = [dp, dp]
     lib.wg_hafnian_noalloc.argtypes = [vp, i32, i32, ip, i32, i32, vp, vp]
     lib.wg_state_create.argtypes = [dp, dp, i32, ctypes.POINTER(vp)]
+    lib.wg_state_create_from_cov.argtypes = [dp, dp, i32, ctypes.c_double, ctypes.POINTER(vp), dp, dp, dp]
     lib.wg_state_destroy.argtypes = [vp]
     lib.wg_plan_create_requests.argtypes = [vp, ctypes.POINTER(WgRequest), i32, i32,
                                             ctypes.POINTER(WgPlanOptions), ctypes.POINTER(vp)]
@@ -440,6 +442,28 @@ def measure_fp_peaks():
 
 class DeviceState:
     """A loop-hafnian source matrix B (M x M) and loop weights gamma (M) resident on the GPU."""
+
+    @classmethod
+    def from_cov(cls, cov, mu, hbar=2.0):
+        """The state formed on the device from a pure state's xp covariance and means
+        (``wg_state_create_from_cov``); returns (state, vacuum amplitude, B, gamma) with host
+        copies of B and gamma."""
+        self = cls.__new__(cls)
+        self.lib = load()
+        cov = np.ascontiguousarray(cov, dtype=np.float64)
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        M = cov.shape[0] // 2
+        dp = ctypes.POINTER(ctypes.c_double)
+        vac = np.zeros(2)
+        B = np.zeros((M, M), dtype=np.complex128)
+        g = np.zeros(M, dtype=np.complex128)
+        h = ctypes.c_void_p()
+        check(self.lib.wg_state_create_from_cov(cov.ctypes.data_as(dp), mu.ctypes.data_as(dp), M, float(hbar),
+                                                ctypes.byref(h), vac.ctypes.data_as(dp), B.ctypes.data_as(dp),
+                                                g.ctypes.data_as(dp)))
+        self.handle = h
+        self.M = M
+        return self, complex(vac[0], vac[1]), B, g
 
     def __init__(self, B, gamma):
         self.lib = load()

@@ -22,6 +22,7 @@
 #include "../../include/walrus_gb300.h"
 #include "host_common.h"
 #include "sieve_kernel.cuh"
+#include "state_glue.cuh"
 
 namespace wg {
 
@@ -1031,6 +1032,65 @@ int wg_state_create(const double* B, const double* gamma, int M, wg_state** stat
   }
   CK(cudaMemcpy(st->d_B, B, sizeof(c64) * (size_t)M * M, cudaMemcpyHostToDevice));
   CK(cudaMemcpy(st->d_gamma, gamma, sizeof(c64) * M, cudaMemcpyHostToDevice));
+  *state = st;
+  return WG_OK;
+}
+
+int wg_state_create_from_cov(const double* cov, const double* mu, int M, double hbar, wg_state** state,
+                             double vacuum[2], double* B_out, double* gamma_out) {
+  if (!state || !cov || !mu || !vacuum || M < 1 || M > 512 || !(hbar > 0))
+    return fail(WG_EINVAL, "bad state arguments (1 <= M <= 512 modes, hbar > 0)");
+  *state = nullptr;
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  const int n = 2 * M;
+  double *d_cov = nullptr, *d_mu = nullptr, *d_out = nullptr;
+  c64 *d_Q = nullptr, *d_X = nullptr;
+  wg_state* st = new wg_state();
+  st->M = M;
+  auto release = [&]() {
+    if (d_cov) cudaFree(d_cov);
+    if (d_mu) cudaFree(d_mu);
+    if (d_out) cudaFree(d_out);
+    if (d_Q) cudaFree(d_Q);
+    if (d_X) cudaFree(d_X);
+  };
+  auto abandon = [&](int code, const char* what) {
+    cudaGetLastError();
+    release();
+    if (st->d_B) cudaFree(st->d_B);
+    if (st->d_gamma) cudaFree(st->d_gamma);
+    delete st;
+    return fail(code, "%s", what);
+  };
+  if (cudaMalloc(&st->d_B, sizeof(c64) * (size_t)M * M) != cudaSuccess ||
+      cudaMalloc(&st->d_gamma, sizeof(c64) * M) != cudaSuccess ||
+      cudaMalloc(&d_cov, sizeof(double) * (size_t)n * n) != cudaSuccess ||
+      cudaMalloc(&d_mu, sizeof(double) * n) != cudaSuccess || cudaMalloc(&d_out, sizeof(double) * 8) != cudaSuccess ||
+      cudaMalloc(&d_Q, sizeof(c64) * (size_t)n * n) != cudaSuccess ||
+      cudaMalloc(&d_X, sizeof(c64) * (size_t)n * M) != cudaSuccess)
+    return abandon(WG_ENOMEM, "state allocation failed");
+  if (cudaMemcpy(d_cov, cov, sizeof(double) * (size_t)n * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(d_mu, mu, sizeof(double) * n, cudaMemcpyHostToDevice) != cudaSuccess)
+    return abandon(WG_ECUDA, "state upload failed");
+  gaussian_state_kernel<<<1, 1024>>>(d_cov, d_mu, M, hbar, d_Q, d_X, st->d_B, st->d_gamma, d_out);
+  double out[8] = {0};
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpy(out, d_out, sizeof(double) * 5, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return abandon(WG_ECUDA, "state kernel failed");
+  if (out[4] != 0.0) return abandon(WG_EINVAL, "covariance is not a physical state: its Husimi matrix Q is not positive definite");
+  st->gamma.resize(M);
+  if (cudaMemcpy(st->gamma.data(), st->d_gamma, sizeof(c64) * M, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return abandon(WG_ECUDA, "state readback failed");
+  if (B_out && cudaMemcpy(B_out, st->d_B, sizeof(c64) * (size_t)M * M, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return abandon(WG_ECUDA, "state readback failed");
+  if (gamma_out) memcpy(gamma_out, st->gamma.data(), sizeof(c64) * M);
+  release();
+  const double rs = out[3];
+  if (rs > 0 && std::isfinite(rs)) st->alpha = std::exp2(-std::round(std::log2(rs)));
+  // <0|psi> = exp(-quad / 2) / det(Q)^(1/4)
+  const double mag = std::exp(-0.5 * out[1] - 0.25 * out[0]);
+  vacuum[0] = mag * std::cos(-0.5 * out[2]);
+  vacuum[1] = mag * std::sin(-0.5 * out[2]);
   *state = st;
   return WG_OK;
 }

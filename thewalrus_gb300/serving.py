@@ -9,8 +9,14 @@ det(Q)^(-1/4) written as det(I - B B^*)^(1/4) for a pure state.
 
 Serving loop (``ProbabilityServer.serve``):
 * requests arrive at their timestamps (Poisson streams in the benchmark);
-* a batch is formed from the pending requests of one state, oldest first, as long as a stream
-  slot is free and the batch's device memory fits the budget (admission by device memory);
+* a batch is formed from the pending requests of one state as long as a stream slot is free and
+  the batch's device memory fits the budget (admission by device memory).  With
+  ``order="cost"`` (the default) pending requests are taken cheapest first -- the cost of a
+  request is its sieve term count times (m + 1)^3 for its largest term matrix, known from the
+  pattern before any work -- and a batch closes once its summed cost passes ``batch_cost``
+  (about 25 ms of GPU work), so that small requests are not held back by a large one in the
+  same plan (a plan answers all its members when its last term is done); ``order="arrival"``
+  takes them oldest first with no cost limit;
 * each batch is a plan whose loop-hafnian matrices are formed on the device from the resident
   state (gather kernel), executed on its own CUDA stream with stream-ordered memory, so batches
   admitted while others run overlap on the GPU;
@@ -20,7 +26,6 @@ latency and hafnians/s.
 """
 import math
 import time
-from collections import deque
 
 import numpy as np
 
@@ -64,6 +69,20 @@ class GaussianState:
         obj = cls(B, alpha)
         quad = np.vdot(alpha, alpha).real - alpha.conj() @ B @ alpha.conj()
         obj.vacuum = np.exp(-0.5 * quad) / np.sqrt(np.sqrt(np.linalg.det(Q)))
+        return obj
+
+    @classmethod
+    def from_cov_on_device(cls, mu, cov, hbar=2):
+        """``from_cov`` with the conversions on the GPU: the Husimi matrix, its Cholesky factor,
+        the columns of Q^-1 that B needs, gamma and the vacuum amplitude are formed by one kernel
+        from the covariance (``wg_state_create_from_cov``), and the state stays resident for the
+        serving plans; B and gamma come back to the host only as copies."""
+        dev, vacuum, B, gamma = nat.DeviceState.from_cov(cov, mu, hbar)
+        obj = cls.__new__(cls)
+        obj.B, obj.gamma, obj.M = B, gamma, B.shape[0]
+        obj.alpha = (np.asarray(mu[:obj.M]) + 1j * np.asarray(mu[obj.M:])) / np.sqrt(2 * hbar)
+        obj.vacuum = vacuum
+        obj.device = dev
         return obj
 
     @classmethod
@@ -123,7 +142,8 @@ def poisson_requests(states, rate, count, photons=(8, 44), seed=0, max_rep=2):
 class ProbabilityServer:
     """Continuous batching of probability requests over CUDA streams (see module docstring)."""
 
-    def __init__(self, states, precision="fp64", max_batch=128, streams=3, mem_budget=None, chunk_scale=1.0):
+    def __init__(self, states, precision="fp64", max_batch=128, streams=3, mem_budget=None, chunk_scale=1.0,
+                 order="cost", batch_cost=4e9):
         import torch
 
         self.torch = torch
@@ -138,6 +158,25 @@ class ProbabilityServer:
             free, _ = torch.cuda.mem_get_info()
             mem_budget = int(0.25 * free)
         self.mem_budget = int(mem_budget)
+        if order not in ("cost", "arrival"):
+            raise ValueError("order must be 'cost' or 'arrival'")
+        self.order = order
+        self.batch_cost = float(batch_cost)
+
+    @staticmethod
+    def request_cost(triple):
+        """Relative GPU work of a request from its pairing (x, edge_reps, oddmode): sieve terms
+        (loop kind: the first radix halved unless there is an unpaired mode) times (m + 1)^3 for
+        the largest bordered term matrix, m = 2 * (edges with a nonzero repetition)."""
+        _, reps, odd = triple
+        reps = [int(r) for r in reps]
+        if not reps:
+            return 0.0
+        steps = float((reps[0] + 2) // 2 if odd is None else reps[0] + 1)
+        for r in reps[1:]:
+            steps *= r + 1
+        m = 2 * sum(1 for r in reps if r > 0)
+        return steps * float(m + 2) ** 3
 
     @staticmethod
     def estimate_bytes(N):
@@ -154,7 +193,8 @@ class ProbabilityServer:
         torch = self.torch
         R = len(requests)
         results = [None] * R
-        pending = deque()
+        pending = []  # waiting requests (indices), non-trivial ones only
+        info = {}  # request -> (cost, pairing, photons)
         inflight = []
         free = list(range(len(self.streams)))
         mem_used = 0
@@ -168,9 +208,18 @@ class ProbabilityServer:
                 raise TimeoutError("serving did not finish within %.0f s" % timeout)
             progressed = False
             while nxt < R and requests[nxt][0] * time_scale <= now:
-                pending.append(nxt)
+                j = nxt
                 nxt += 1
                 progressed = True
+                _, sidx, pat = requests[j]
+                triv = self.states[sidx].trivial_loop_hafnian(pat)
+                if triv is not None:  # no photons or one: answered without the sieve
+                    self._finish(results, requests, j, triv, time.perf_counter() - t0, -1, time_scale)
+                    done += 1
+                    continue
+                triple = matched_reps(pat)
+                info[j] = (self.request_cost(triple), triple, int(np.sum(pat)))
+                pending.append(j)
             # completions
             for fl in list(inflight):
                 if fl["event"].query():
@@ -184,34 +233,35 @@ class ProbabilityServer:
                     free.append(fl["slot"])
                     inflight.remove(fl)
                     progressed = True
-            # admission of a new batch: one state, oldest first, within slots and memory
+            # admission of a new batch: one state; cheapest (or oldest) first, within the cost
+            # budget, the slots and the device memory
             if free and pending:
+                if self.order == "cost":
+                    pending.sort(key=lambda j: (info[j][0], j))
                 sidx = requests[pending[0]][1]
-                batch, est = [], 0
-                keep = deque()
-                while pending and len(batch) < self.max_batch:
-                    j = pending.popleft()
-                    if requests[j][1] != sidx:
+                batch, est, work = [], 0, 0.0
+                keep = []
+                closed = False
+                for j in pending:
+                    if closed or len(batch) >= self.max_batch or requests[j][1] != sidx:
                         keep.append(j)
                         continue
-                    pat = requests[j][2]
-                    st = self.states[sidx]
-                    triv = st.trivial_loop_hafnian(pat)
-                    if triv is not None:
-                        self._finish(results, requests, j, triv, time.perf_counter() - t0, -1, time_scale)
-                        done += 1
-                        continue
-                    e = self.estimate_bytes(int(np.sum(pat)))
-                    if batch and mem_used + est + e > self.mem_budget:
+                    cost, _, photons = info[j]
+                    e = self.estimate_bytes(photons)
+                    over_mem = batch and mem_used + est + e > self.mem_budget
+                    over_cost = batch and self.order == "cost" and work + cost > self.batch_cost
+                    if over_mem or over_cost:
                         keep.append(j)
-                        break
+                        closed = True
+                        continue
                     batch.append(j)
                     est += e
-                pending = keep + pending
+                    work += cost
+                pending = keep
                 if batch:
                     slot = free.pop()
                     stream = self.streams[slot]
-                    triples = [matched_reps(requests[j][2]) for j in batch]
+                    triples = [info[j][1] for j in batch]
                     plan = nat.Plan.from_requests(self.states[sidx].device, triples, self.precision,
                                                   chunk_scale=self.chunk_scale, stream=stream.cuda_stream)
                     plan.execute(stream.cuda_stream)
