@@ -192,6 +192,13 @@ long long wg_plan_device_bytes(const wg_plan* plan);
 /* Device-time microbenchmark of the FP64 and FP32 FMA pipes (TFLOP/s, 2 flops per FMA). */
 int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
 
+/* The kernels' own arithmetic primitives evaluated elementwise on the device, for checks against
+ * IEEE and exact references (no counterpart in the reference): op 0 the pivot reciprocal 1/x
+ * (approximate reciprocal + two Newton steps), 1 the double-double reciprocal of (x, x_lo), 2 the
+ * double-double quotient (x, x_lo) / k with k = (int)y, 3 the double-double product of (x, x_lo)
+ * and (y, y_lo).  in: 4 doubles per element (x, x_lo, y, y_lo); out: 2 per element (hi, lo). */
+int wg_check_arith(int op, const double* in, int n, double* out);
+
 /* Allocation-free plain hafnian (FP64 terms).  No counterpart in the reference: it exists for
  * callers that cannot allocate device memory while they call us -- code that runs inside its own
  * memory pool or arena, serving plugins that forbid allocation on the request path, and loops

@@ -79,3 +79,25 @@ def test_state_formed_on_the_device_from_the_covariance(golden):
     # a covariance whose Husimi matrix is not positive definite (negative variances) is refused
     with pytest.raises(RuntimeError):
         GaussianState.from_cov_on_device(np.zeros(8), -2.0 * np.eye(8))
+
+
+def test_served_many_photon_requests_vs_double_double():
+    """Served amplitudes of 26-32-photon requests on 64-mode states (12-13 sieve edges, term
+    matrices of up to 26 rows plus the border) against the double-double sieve of the same loop
+    hafnian: within 1e-10, or 64 eps cond where the sum's condition number cond = sum|term| /
+    |sum| (the oracle's, ~1e3..1e4 here) allows more."""
+    pytest.importorskip("torch")
+    import thewalrus_gb300 as tw
+    states = [GaussianState.synthetic(modes=64, seed=s) for s in range(2)]
+    reqs = poisson_requests(states, rate=1e5, count=6, photons=(26, 32), seed=11)
+    srv = ProbabilityServer(states, max_batch=8, streams=2)
+    res = srv.serve(reqs)
+    for (t, s, pat), r in zip(reqs, res):
+        st = states[s]
+        truth = complex(tw.hafnian_repeated(st.B, list(pat), mu=st.gamma, loop=True, precision="dd"))
+        p = tw.prepare_loop_hafnian(st.B, st.gamma, list(pat))
+        N = int(np.sum(pat))
+        cond = complex(oracle.sieve_term_range(p.A, p.reps, Dx=p.D, absolute=True)).real * 0.5 ** (N // 2 - 1) / abs(truth)
+        tol = max(RTOL, 64 * 2.0 ** -53 * cond)
+        got = r["amplitude"] / st.norm(pat)
+        assert abs(got - truth) <= tol * abs(truth), (N, got, truth, cond)

@@ -120,6 +120,7 @@ EXPORTS = [
     "wg_plan_destroy", "wg_run",
     "wg_measure_fp_peaks", "wg_hafnian_noalloc", "wg_state_create", "wg_state_destroy",
     "wg_plan_create_requests", "wg_plan_device_bytes", "wg_instance_terms", "wg_state_create_from_cov",
+    "wg_check_arith",
 ]
 
 
@@ -169,6 +170,7 @@ def load(build_if_needed=True):
     lib.wg_plan_destroy.argtypes = [vp]
     lib.wg_run.argtypes = [ctypes.POINTER(WgInstance), i32, i32, dp, vp]
     lib.wg_measure_fp_peaks.argtypes = [dp, dp]
+    lib.wg_check_arith.argtypes = [i32, dp, i32, dp]
     lib.wg_hafnian_noalloc.argtypes = [vp, i32, i32, ip, i32, i32, vp, vp]
     lib.wg_state_create.argtypes = [dp, dp, i32, ctypes.POINTER(vp)]
     lib.wg_state_create_from_cov.argtypes = [dp, dp, i32, ctypes.c_double, ctypes.POINTER(vp), dp, dp, dp]
@@ -430,6 +432,20 @@ def run(instances, precision="fp64", stream=0):
     check(lib.wg_run(arr, len(insts), PRECISIONS[precision],
                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_void_p(stream)))
     return (out[0::2] + 1j * out[1::2])[:total]
+
+
+def check_arith(op, x, x_lo=None, y=None, y_lo=None):
+    """Evaluate one of the kernels' arithmetic primitives on the device elementwise
+    (``wg_check_arith``); returns the (hi, lo) arrays."""
+    x = np.asarray(x, dtype=np.float64).ravel()
+    z = np.zeros_like(x)
+    inp = np.ascontiguousarray(np.stack([x, z if x_lo is None else np.asarray(x_lo, dtype=np.float64).ravel(),
+                                         z if y is None else np.asarray(y, dtype=np.float64).ravel(),
+                                         z if y_lo is None else np.asarray(y_lo, dtype=np.float64).ravel()], axis=1))
+    out = np.zeros((len(x), 2))
+    dp = ctypes.POINTER(ctypes.c_double)
+    check(load().wg_check_arith(int(op), inp.ctypes.data_as(dp), len(x), out.ctypes.data_as(dp)))
+    return out[:, 0], out[:, 1]
 
 
 def measure_fp_peaks():

@@ -1205,6 +1205,49 @@ int wg_loop_hafnian_batch(const void* A, const void* D, int n, int dtype, const 
   return wg_run(&in, 1, precision, out, stream);
 }
 
+// Device arithmetic primitives of the kernels, evaluated elementwise for checks against IEEE and
+// exact references: 0 recip_newton(x); 1 dd_recip((x, lo)) -> (hi, lo); 2 dd_div_int((x, lo), k)
+// with k = (int)y -> (hi, lo); 3 dd_mul((x, lo), (y, lo2)) -> (hi, lo).  Inputs per element:
+// in[4i .. 4i+3] = x, x_lo, y, y_lo; outputs out[2i], out[2i+1].
+static __global__ void arith_check_kernel(int op, const double* __restrict__ in, int n, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double x = in[4 * i], xl = in[4 * i + 1], y = in[4 * i + 2], yl = in[4 * i + 3];
+  ddr r = {0.0, 0.0};
+  switch (op) {
+    case 0: r.hi = recip_newton(x); break;
+    case 1: r = dd_recip({x, xl}); break;
+    case 2: r = dd_div_int({x, xl}, (int)y); break;
+    default: r = dd_mul({x, xl}, {y, yl}); break;
+  }
+  out[2 * i] = r.hi;
+  out[2 * i + 1] = r.lo;
+}
+
+int wg_check_arith(int op, const double* in, int n, double* out) {
+  if (op < 0 || op > 3 || n < 0 || (n > 0 && (!in || !out))) return fail(WG_EINVAL, "bad arithmetic check arguments");
+  if (n == 0) return WG_OK;
+  int rc = ensure_init(-1);
+  if (rc) return rc;
+  double *d_in = nullptr, *d_out = nullptr;
+  if (cudaMalloc(&d_in, sizeof(double) * 4 * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&d_out, sizeof(double) * 2 * (size_t)n) != cudaSuccess) {
+    cudaGetLastError();
+    if (d_in) cudaFree(d_in);
+    return fail(WG_ENOMEM, "arithmetic check allocation failed");
+  }
+  cudaError_t e = cudaMemcpy(d_in, in, sizeof(double) * 4 * (size_t)n, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    arith_check_kernel<<<(n + 255) / 256, 256>>>(op, d_in, n, d_out);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out, d_out, sizeof(double) * 2 * (size_t)n, cudaMemcpyDeviceToHost);
+  cudaFree(d_in);
+  cudaFree(d_out);
+  if (e != cudaSuccess) return fail(WG_ECUDA, "arithmetic check: %s", cudaGetErrorString(e));
+  return WG_OK;
+}
+
 int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops) {
   int rc = ensure_init(-1);
   if (rc) return rc;
