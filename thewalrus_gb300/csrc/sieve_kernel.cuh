@@ -205,38 +205,11 @@ __device__ __forceinline__ void phase_b_rows(S* __restrict__ W, const S* __restr
 #pragma unroll
   for (int k = 0; k < NF; ++k) acc[k] = A::zero();
   const bool live = !PARTIAL || lane + 32 * (NF - 1) < rows;
-  if constexpr (!A::fp64) {
-    // double-float: a multiply-add is a ~14-deep chain of dependent FP32 operations, and with one
-    // row per lane the sum over b is one such chain per row -- latency, not the FP32 pipe, set
-    // its pace.  Even and odd b go to two partial sums, added at the end.
-    S acc2[NF];
+  for (int b = j + 1; b < mb; ++b) {
+    const S xb = xv[b];
 #pragma unroll
-    for (int k = 0; k < NF; ++k) acc2[k] = A::zero();
-    int b = j + 1;
-    for (; b + 1 < mb; b += 2) {
-      const S x0 = xv[b], x1 = xv[b + 1];
-#pragma unroll
-      for (int k = 0; k < NF; ++k)
-        if (k < NF - 1 || live) {
-          acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], x0, acc[k]);
-          acc2[k] = A::fma(W[(lane + 32 * k) * ldw + b + 1], x1, acc2[k]);
-        }
-    }
-    if (b < mb) {
-      const S x0 = xv[b];
-#pragma unroll
-      for (int k = 0; k < NF; ++k)
-        if (k < NF - 1 || live) acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], x0, acc[k]);
-    }
-#pragma unroll
-    for (int k = 0; k < NF; ++k) acc[k] = A::add(acc[k], acc2[k]);
-  } else {
-    for (int b = j + 1; b < mb; ++b) {
-      const S xb = xv[b];
-#pragma unroll
-      for (int k = 0; k < NF; ++k)
-        if (k < NF - 1 || live) acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], xb, acc[k]);
-    }
+    for (int k = 0; k < NF; ++k)
+      if (k < NF - 1 || live) acc[k] = A::fma(W[(lane + 32 * k) * ldw + b], xb, acc[k]);
   }
 #pragma unroll
   for (int k = 0; k < NF; ++k)
@@ -584,16 +557,12 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
             --left;
           }
         } else {
-        // double-float: the odd steps of a piece go to a second sum (two dependent chains in
-        // flight instead of one), added when the piece ends
-        S accB = A::zero();
         for (int it = 0; it < tot; ++it) {
           const int q = (it >= l0) + (it >= l0 + l1);
           const int start = q == 0 ? 0 : (q == 1 ? l0 : l0 + l1);
           if (it == start && it > 0) {
-            part[3 * lane + q - 1] = A::fp64 ? acc : A::add(acc, accB);
+            part[3 * lane + q - 1] = acc;
             acc = A::zero();
-            accB = A::zero();
           }
           const int row = (sc.rowmask >> q) & 1;
           const int j = q == 0 ? sc.j[0] : (q == 1 ? sc.j[1] : sc.j[2]);
@@ -603,11 +572,9 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
             if (slot < 0) slot += kw;
             const S cv = cw_at(W, ldw, nb, win, kw, tile, i + row - r - 1, slot, j - r - 1);
             const S tr = A::fp64 ? W[(wi + row - r) * ldw + wi + row] : tb[row * kw + r];
-            if (!A::fp64 && ((it - start) & 1)) accB = A::fma(tr, cv, accB);
-            else acc = A::fma(tr, cv, acc);
+            acc = A::fma(tr, cv, acc);
           }
         }
-        if constexpr (!A::fp64) acc = A::add(acc, accB);
         }
         if (tot > 0) part[3 * lane + (l2 > 0 ? 2 : (l1 > 0 ? 1 : 0))] = acc;
       }
