@@ -143,6 +143,11 @@ int wg_plan_create_ex(const wg_instance* inst, int count, int precision, const w
                       wg_plan** plan);
 int wg_plan_execute(wg_plan* plan, void* stream);
 int wg_plan_read(wg_plan* plan, double* out, void* stream);
+/* Per output of the last execution: the sum over sieve terms of |prefactor x term| (real plus
+ * imaginary magnitude) times the output's final scale, i.e. the size of the terms the result
+ * cancels from.  magnitude / |result| is the sum's condition number: the result's rounding error
+ * is about (the terms' relative rounding) x magnitude.  0 for the exact precisions. */
+int wg_plan_read_magnitudes(wg_plan* plan, double* out, void* stream);
 int wg_plan_outputs(const wg_plan* plan);
 int wg_plan_kernel_launches(const wg_plan* plan);
 /* Diagnostics for chunk-level checks.  wg_plan_partials copies the unscaled per-chunk partial

@@ -19,6 +19,8 @@ from ._hafnian import (
     prepare_loop_hafnian,
     prepare_loop_hafnian_batch,
     prepare_loop_hafnian_batch_gamma,
+    hafnian_with_error,
+    run_with_magnitudes,
 )
 from . import _native as native
 
@@ -38,6 +40,8 @@ __all__ = [
     "prepare_loop_hafnian",
     "prepare_loop_hafnian_batch",
     "prepare_loop_hafnian_batch_gamma",
+    "hafnian_with_error",
+    "run_with_magnitudes",
     "native",
     "version",
 ]

@@ -14,7 +14,8 @@ Same names, arguments, return conventions and errors as the reference's public f
 The host keeps validation, the closed forms for tiny matrices, edge pairing and reordering;
 every sieve runs on the GPU (no CPU fallback).  Extra keyword ``precision`` selects "fp64"
 (default), "df" (FP32 double-float term arithmetic), "dd" (FP64 double-double terms, for sums
-that cancel beyond FP64's reach) or "exact" (integer inputs).  Sieve results come back as
+that cancel beyond FP64's reach), "auto" (FP64, and double-double again for the instances whose
+term magnitudes say FP64 may miss 1e-10) or "exact" (integer inputs).  Sieve results come back as
 ``numpy.complex128`` also for real input, as in the reference.
 """
 import numpy as np
@@ -33,6 +34,8 @@ __all__ = [
     "prepare_hafnian",
     "prepare_loop_hafnian",
     "prepare_loop_hafnian_batch",
+    "hafnian_with_error",
+    "run_with_magnitudes",
 ]
 
 DEFAULT_PRECISION = "fp64"
@@ -248,10 +251,77 @@ def prepare_loop_hafnian(A, D=None, reps=None, glynn=True):
     return nat.Instance(nat.WG_KIND_LOOP, Ax, edge_reps, glynn=glynn, D=Dx, oddV=oddV, oddloop=oddloop)
 
 
+# Relative rounding of one sieve term in each term arithmetic (the unit roundoff of its
+# significand) and the rule of precision="auto": FP64 first; when AUTO_FACTOR x 2^-53 x
+# sum|term| exceeds AUTO_RTOL x |result| the instance runs again in double-double.  The factor
+# covers the Hessenberg route's per-term rounding, ~15x the unit roundoff at the median: on the
+# n = 40 benchmark matrices (sum|term| / |sum| = 6.8e4 complex, 2.0e5 real) FP64 ends 4.6e-12
+# and 4.6e-11 from the reference's values, on the 40-photon loop hafnian of a 20-mode state
+# (3.4e10) 1.8e-6; the first stays FP64, the other two go to double-double.
+UNIT_ROUNDOFF = {"fp64": 2.0 ** -53, "df": 2.0 ** -48, "dd": 2.0 ** -104}
+AUTO_FACTOR = 8.0
+AUTO_RTOL = 1e-10
+
+
+def run_with_magnitudes(instances, precision="fp64"):
+    """Outputs of the instances with, per output, sum |prefactor x term| times the final scale
+    (the size of the terms the output cancels from): (values, magnitudes)."""
+    plan = nat.Plan(list(instances), precision=precision)
+    try:
+        plan.execute()
+        return plan.read(), plan.read_magnitudes()
+    finally:
+        plan.close()
+
+
+def _auto_run(insts):
+    """precision="auto": FP64, then double-double for the instances whose FP64 rounding could
+    exceed AUTO_RTOL relative (see UNIT_ROUNDOFF)."""
+    vals, mags = run_with_magnitudes(insts, "fp64")
+    outs = [inst.outputs() for inst in insts]
+    redo, off = [], 0
+    for k, n_out in enumerate(outs):
+        v, m = vals[off:off + n_out], mags[off:off + n_out]
+        scale = max(float(np.max(np.abs(v))), 1e-300)
+        if AUTO_FACTOR * UNIT_ROUNDOFF["fp64"] * float(np.max(m)) > AUTO_RTOL * scale:
+            redo.append((k, off))
+        off += n_out
+    if redo:
+        again = nat.run([insts[k] for k, _ in redo], "dd")
+        pos = 0
+        for k, o in redo:
+            vals[o:o + outs[k]] = again[pos:pos + outs[k]]
+            pos += outs[k]
+    return vals
+
+
+def _run(insts, precision):
+    if precision == "auto":
+        if all(_integral(i) for i in insts) and nat.exact_primes(insts) is not None:
+            return nat.run(insts, "exact")
+        return _auto_run(insts)
+    return nat.run(insts, precision)
+
+
 def _finish(prep, precision):
     if not isinstance(prep, nat.Instance):
         return prep
-    return np.complex128(nat.run([prep], precision)[0])
+    return np.complex128(_run([prep], precision)[0])
+
+
+def hafnian_with_error(A, loop=False, rtol=1e-05, atol=1e-08, precision="fp64"):
+    """(hafnian, error estimate, magnitude): the sieve result with the sum over its terms of
+    |prefactor x term| (the magnitude the result cancels from) and the first-order estimate of
+    its rounding error, the term arithmetic's unit roundoff times that magnitude (the measured
+    errors of the FP64 sieve lie within 16x of it).  For a small matrix answered in closed form
+    the estimate and magnitude are 0.  ``precision``: "fp64", "df" or "dd"."""
+    input_validation(A, rtol=rtol, atol=atol)
+    done, value = _closed_form(A, loop, rtol, atol)
+    prep = None if done else (prepare_loop_hafnian(A, None, None, True) if loop else prepare_hafnian(A))
+    if done or not isinstance(prep, nat.Instance):
+        return np.complex128(value if done else prep), 0.0, 0.0
+    vals, mags = run_with_magnitudes([prep], precision)
+    return np.complex128(vals[0]), float(UNIT_ROUNDOFF[precision] * mags[0]), float(mags[0])
 
 
 def _haf(A, reps=None, glynn=True, precision=None):
@@ -310,8 +380,9 @@ def hafnian(A, loop=False, rtol=1e-05, atol=1e-08, approx=False, num_samples=100
     hafnian always uses the finite-difference sieve, as in the reference).  ``precision``:
     None (exact for integer-valued real inputs, FP64 otherwise), "fp64", "df" (double-float
     terms), "dd" (double-double terms: ~14x the FP64 time, for sieve sums whose terms cancel by
-    more than ~1e6, e.g. the loop hafnians of many-photon Gaussian-state patterns) or "exact"
-    (integer inputs only).
+    more than ~1e6, e.g. the loop hafnians of many-photon Gaussian-state patterns), "auto"
+    (FP64, re-run in double-double when the sum of the terms' magnitudes says FP64 may miss
+    1e-10) or "exact" (integer inputs only).
     """
     input_validation(A, rtol=rtol, atol=atol)
     glynn = _method_glynn(method) if not loop else True
@@ -397,7 +468,7 @@ def prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True):
 def loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True, precision=None):
     """Loop hafnians for every photon number 0..N_cutoff of the last mode, in one sieve."""
     prep = prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn)
-    return nat.run([prep], _auto(precision, [prep]))
+    return _run([prep], _auto(precision, [prep]))
 
 
 def prepare_loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True):
@@ -422,7 +493,7 @@ def loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn=True, precision=N
     preps = prepare_loop_hafnian_batch_gamma(A, D, fixed_reps, N_cutoff, glynn)
     if not preps:
         return np.zeros((0, N_cutoff + 1), dtype=np.complex128)
-    vals = nat.run(preps, _auto(precision, preps))
+    vals = _run(preps, _auto(precision, preps))
     return vals.reshape(len(preps), -1)
 
 
@@ -450,7 +521,7 @@ def hafnian_batch(matrices, loop=False, rtol=1e-05, atol=1e-08, method="glynn", 
         else:
             results[i] = prep
     if insts:
-        vals = nat.run(insts, _auto(precision, insts))
+        vals = _run(insts, _auto(precision, insts))
         for i, v in zip(where, vals):
             results[i] = np.complex128(v)
     return results

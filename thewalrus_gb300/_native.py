@@ -120,7 +120,7 @@ EXPORTS = [
     "wg_plan_destroy", "wg_run",
     "wg_measure_fp_peaks", "wg_hafnian_noalloc", "wg_state_create", "wg_state_destroy",
     "wg_plan_create_requests", "wg_plan_device_bytes", "wg_instance_terms", "wg_state_create_from_cov",
-    "wg_check_arith",
+    "wg_check_arith", "wg_plan_read_magnitudes",
 ]
 
 
@@ -161,6 +161,7 @@ def load(build_if_needed=True):
                                       ctypes.POINTER(vp)]
     lib.wg_plan_execute.argtypes = [vp, vp]
     lib.wg_plan_read.argtypes = [vp, dp, vp]
+    lib.wg_plan_read_magnitudes.argtypes = [vp, dp, vp]
     lib.wg_plan_outputs.argtypes = [vp]
     lib.wg_plan_kernel_launches.argtypes = [vp]
     lib.wg_plan_transfer_bytes.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
@@ -371,6 +372,14 @@ class Plan:
         check(self.lib.wg_plan_read(self.handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                     ctypes.c_void_p(stream)))
         return (out[0::2] + 1j * out[1::2])[: self.total_out]
+
+    def read_magnitudes(self, stream=0):
+        """Per output of the last execution: sum |prefactor x term| times the final scale (the
+        size of the terms the output cancels from; 0 for exact precisions)."""
+        out = np.zeros(max(self.total_out, 1))
+        check(self.lib.wg_plan_read_magnitudes(self.handle, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                               ctypes.c_void_p(stream)))
+        return out[: self.total_out]
 
     def close(self):
         if getattr(self, "handle", None):

@@ -156,6 +156,7 @@ struct wg_plan {
   double2* d_partials = nullptr;
   double* d_scales = nullptr;
   double2* d_out = nullptr;
+  double* d_mag = nullptr;  // per output: sum |prefactor x term| x |final scale|
   unsigned int* d_counters = nullptr;
   int* d_err = nullptr;
   bool use_graph = false;
@@ -683,7 +684,12 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
       const double tc = P[i].term_cost;
       const long long hi = P[i].t_hi, pmin = std::max(1LL, (long long)std::ceil(min_cost / tc));
       d.part_base = nparts;
-      d.pstride = stype_dd(P[i].stype) ? 2 * d.nout : d.nout;  // dd: sums and compensations
+      // slots per chunk: sums; double-double kinds their compensations; floating-point kinds
+      // the term magnitudes (the exact sieve's residues have none)
+      const bool dd = stype_dd(P[i].stype), fl = !stype_mod(P[i].stype);
+      d.comp_off = dd ? d.nout : 0;
+      d.mag_off = fl ? (dd ? 2 : 1) * d.nout : 0;
+      d.pstride = (1 + (dd ? 1 : 0) + (fl ? 1 : 0)) * d.nout;
       int nch = 0;
       for (long long t = P[i].t_lo; t < hi; ++nch) {
         const double want = std::min(remaining / div, kMaxChunkCost * chunk_scale);
@@ -716,11 +722,13 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
   const size_t b_parts = al(sizeof(double2) * std::max(nparts, 1));
   const size_t b_scales = al(sizeof(double) * std::max<size_t>(scales.size(), 1));
   const size_t b_out = al(sizeof(double2) * std::max(out, 1));
+  const size_t b_mag = al(sizeof(double) * std::max(out, 1));
   const size_t b_cnt = al(sizeof(unsigned int) * std::max<size_t>(pl->groups.size(), 1));
   const size_t b_err = al(sizeof(int));
   const size_t b_gdesc = gs ? al(sizeof(GatherDev) * std::max<size_t>(gs->desc.size(), 1)) : 0;
   const size_t b_gidx = gs ? al(sizeof(int) * std::max<size_t>(gs->idx.size(), 1)) : 0;
-  const size_t total = b_inst + b_chunks + b_pool + b_parts + b_scales + b_out + b_cnt + b_err + b_gdesc + b_gidx;
+  const size_t total =
+      b_inst + b_chunks + b_pool + b_parts + b_scales + b_out + b_mag + b_cnt + b_err + b_gdesc + b_gidx;
   cudaStream_t cs = (cudaStream_t)opt.stream;
   pl->alloc_stream = cs;
   pl->async_alloc = cs != nullptr;
@@ -737,6 +745,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
   pl->d_partials = (double2*)base; base += b_parts;
   pl->d_scales = (double*)base; base += b_scales;
   pl->d_out = (double2*)base; base += b_out;
+  pl->d_mag = (double*)base; base += b_mag;
   pl->d_counters = (unsigned int*)base; base += b_cnt;
   pl->d_err = (int*)base; base += b_err;
   pl->device_bytes = (long long)total;
@@ -829,7 +838,8 @@ static int launch_plan(wg_plan* pl, cudaStream_t st) {
     const int blocks = (pl->total_out * 32 + threads - 1) / threads;  // one warp per output
     const unsigned int modp = prec_mod(pl->precision) ? MOD_PRIMES[pl->precision - WG_PREC_MOD0] : 0u;
     reduce_kernel<<<std::max(blocks, 1), threads, 0, st>>>(pl->d_inst, ninst, pl->d_partials, pl->d_scales, pl->d_out,
-                                                           pl->d_counters, (int)pl->groups.size(), pl->total_out, modp);
+                                                           pl->d_counters, (int)pl->groups.size(), pl->total_out, modp,
+                                                           pl->d_mag);
     CK(cudaGetLastError());
   }
   return WG_OK;
@@ -977,6 +987,15 @@ int wg_plan_read(wg_plan* plan, double* out, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   if (plan->total_out > 0)
     CK(cudaMemcpyAsync(out, plan->d_out, sizeof(double2) * plan->total_out, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return WG_OK;
+}
+
+int wg_plan_read_magnitudes(wg_plan* plan, double* out, void* stream) {
+  if (!plan || (!out && plan->total_out > 0)) return fail(WG_EINVAL, "NULL argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  if (plan->total_out > 0)
+    CK(cudaMemcpyAsync(out, plan->d_mag, sizeof(double) * plan->total_out, cudaMemcpyDeviceToHost, st));
   CK(cudaStreamSynchronize(st));
   return WG_OK;
 }

@@ -53,8 +53,11 @@ struct InstDev {
   // reduction bookkeeping
   int part_base;   // first partial slot of this instance
   int nchunks;     // chunks of this instance (partials are [part_base, part_base + nchunks*pstride))
-  int pstride;     // partial slots per chunk: nout, or 2 nout (sums, then compensations) for
-                   // double-double kinds; 0 reads as nout
+  int pstride;     // partial slots per chunk (0 reads as nout): the sums, then, when their
+                   // offsets are nonzero, the compensations (double-double kinds) and the term
+                   // magnitudes sum |prefactor x term| (floating-point kinds)
+  int comp_off;    // slot offset of the compensations within a chunk's slots (0: none)
+  int mag_off;     // slot offset of the term magnitudes (0: none)
   int out_base;    // first output slot
   int scale_base;  // first output scale
 };
@@ -855,6 +858,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       }
     }
     double s_re = 0, s_im = 0, k_re = 0, k_im = 0;  // lane o: Neumaier sum of output o
+    double mag = 0;                                   // lane o: sum of |re| + |im| of its terms
     S macc = A::zero();                               // modular kinds: lane o's residue sum
 
     for (long long t = ch.t0; t < ch.t1; ++t) {
@@ -907,6 +911,7 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
           const double xr = pre * z.re, xi = pre * z.im;
           neumaier(s_re, k_re, xr);
           neumaier(s_im, k_im, xi);
+          mag += fabs(xr) + fabs(xi);
           if constexpr (A::dd) {  // the product's rounding error and the low parts join the compensation
             const c64 zl = A::lo_c64(f);
             k_re += ::fma(pre, z.re, -xr) + pre * zl.re;
@@ -1042,13 +1047,17 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
     }
     if constexpr (A::modular) {
       if (lane < nout) P.partials[ch.part + lane] = make_double2((double)A::to_c64(macc).re, 0.0);
-    } else if constexpr (A::dd) {  // sum and compensation kept apart: 2 nout slots per chunk
+    } else if constexpr (A::dd) {  // sum and compensation kept apart
       if (lane < nout) {
         P.partials[ch.part + lane] = make_double2(s_re, s_im);
-        P.partials[ch.part + nout + lane] = make_double2(k_re, k_im);
+        P.partials[ch.part + I.comp_off + lane] = make_double2(k_re, k_im);
+        if (I.mag_off) P.partials[ch.part + I.mag_off + lane] = make_double2(mag, 0.0);
       }
     } else {
-      if (lane < nout) P.partials[ch.part + lane] = make_double2(s_re + k_re, s_im + k_im);
+      if (lane < nout) {
+        P.partials[ch.part + lane] = make_double2(s_re + k_re, s_im + k_im);
+        if (I.mag_off) P.partials[ch.part + I.mag_off + lane] = make_double2(mag, 0.0);
+      }
     }
     __syncwarp();
   }
@@ -1069,7 +1078,7 @@ __device__ __forceinline__ void two_sum_merge(double& s, double& c, double s2, d
 // counters for the next execution.
 static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst, const double2* __restrict__ partials,
                               const double* __restrict__ scales, double2* __restrict__ out, unsigned int* counters,
-                              int ncounters, int total_out, unsigned int modp) {
+                              int ncounters, int total_out, unsigned int modp, double* __restrict__ mags = nullptr) {
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (gw < total_out) {
@@ -1081,18 +1090,21 @@ static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst
     }
     const InstDev& I = inst[lo];
     const int o = gw - I.out_base;
-    double sr = 0, si = 0, cr = 0, ci = 0;
+    double sr = 0, si = 0, cr = 0, ci = 0, ms = 0;
     const int ps = I.pstride > I.nout ? I.pstride : I.nout;  // slots per chunk
     for (int c = lane; c < I.nchunks; c += 32) {
       const double2 v = partials[I.part_base + c * ps + o];
       neumaier(sr, cr, v.x);
       neumaier(si, ci, v.y);
-      if (ps > I.nout) {  // double-double kinds: the chunk's compensation
-        const double2 w = partials[I.part_base + c * ps + I.nout + o];
+      if (I.comp_off) {  // double-double kinds: the chunk's compensation
+        const double2 w = partials[I.part_base + c * ps + I.comp_off + o];
         cr += w.x;
         ci += w.y;
       }
+      if (I.mag_off) ms += partials[I.part_base + c * ps + I.mag_off + o].x;
     }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) ms += __shfl_xor_sync(0xffffffffu, ms, off);
 #pragma unroll
     for (int off = 16; off; off >>= 1) {
       const double osr = __shfl_xor_sync(0xffffffffu, sr, off), ocr = __shfl_xor_sync(0xffffffffu, cr, off);
@@ -1117,6 +1129,7 @@ static __global__ void reduce_kernel(const InstDev* __restrict__ inst, int ninst
       } else {
         out[gw] = make_double2((sr + cr) * sc, (si + ci) * sc);
       }
+      if (mags) mags[gw] = I.mag_off ? ms * fabs(sc) : 0.0;
     }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0)
