@@ -471,11 +471,19 @@ def run_loop(args):
     e2e_s = (time.perf_counter() - t0) / args.steps
     x, reps, odd = tw.matched_reps(list(rpt))
     flops = costmodel.instance_flops(reps, True, kind="loop", odd=odd is not None)
-    print(json.dumps({"metric": "loop hafnians/s (20-mode Gaussian state, 40 photons)", "value": 1 / dev_s,
-                      "unit": "hafnians/s", "ms_per_step": dev_s * 1e3, "e2e": {"value": 1 / e2e_s, "unit": "hafnians/s"},
-                      "edge_reps": [int(r) for r in reps], "terms": int(np.prod([r + 1 for r in reps]) // 1),
-                      "achieved_tflops": flops / dev_s / 1e12, "precision": args.precision,
-                      "result": [float(val.real), float(val.imag)]}), flush=True)
+    line = {"metric": "loop hafnians/s (20-mode Gaussian state, 40 photons)", "value": 1 / dev_s,
+            "unit": "hafnians/s", "ms_per_step": dev_s * 1e3, "e2e": {"value": 1 / e2e_s, "unit": "hafnians/s"},
+            "edge_reps": [int(r) for r in reps], "terms": int(np.prod([r + 1 for r in reps]) // 1),
+            "achieved_tflops": flops / dev_s / 1e12, "precision": args.precision,
+            "result": [float(val.real), float(val.imag)]}
+    # accuracy against the committed _Float128 value, and the sum's condition number
+    path = os.path.join(ROOT, "tests", "golden", "metric_cases.npz")
+    if os.path.exists(path):
+        truth = complex(np.load(path)["lhaf_state20_40/oracle_q"])
+        line["rel_err_vs_float128"] = abs(complex(val) - truth) / abs(truth)
+    vals, mags = tw.run_with_magnitudes([inst], "fp64")
+    line["sum_abs_terms_over_abs_sum"] = float(mags[0] / abs(vals[0]))
+    print(json.dumps(line), flush=True)
 
 
 def run_batch(args):
