@@ -451,7 +451,17 @@ def run_loop(args):
     import thewalrus_gb300 as tw
     from thewalrus_gb300 import costmodel, workloads as wl
 
-    A, gamma, rpt = wl.gaussian_state_loop(modes=20, seed=1, photons=40, max_rep=3)
+    # the committed fixture holds this input as generated for the reference run (the Haar unitary
+    # comes from a QR factorisation, whose last bits differ between LAPACK builds, and this sum
+    # amplifies input differences ~1e10-fold); the generator is the fallback
+    path = os.path.join(ROOT, "tests", "golden", "metric_cases.npz")
+    truth = None
+    if os.path.exists(path):
+        fx = np.load(path)
+        A, gamma, rpt = fx["lhaf_state20_40/A"], fx["lhaf_state20_40/mu"], fx["lhaf_state20_40/rpt"]
+        truth = complex(fx["lhaf_state20_40/oracle_q"])
+    else:
+        A, gamma, rpt = wl.gaussian_state_loop(modes=20, seed=1, photons=40, max_rep=3)
     inst = tw.prepare_loop_hafnian(A, gamma, list(rpt))
     plan = nat.Plan([inst], precision=args.precision)
     s = torch.cuda.current_stream()
@@ -477,9 +487,7 @@ def run_loop(args):
             "achieved_tflops": flops / dev_s / 1e12, "precision": args.precision,
             "result": [float(val.real), float(val.imag)]}
     # accuracy against the committed _Float128 value, and the sum's condition number
-    path = os.path.join(ROOT, "tests", "golden", "metric_cases.npz")
-    if os.path.exists(path):
-        truth = complex(np.load(path)["lhaf_state20_40/oracle_q"])
+    if truth is not None:
         line["rel_err_vs_float128"] = abs(complex(val) - truth) / abs(truth)
     vals, mags = tw.run_with_magnitudes([inst], "fp64")
     line["sum_abs_terms_over_abs_sum"] = float(mags[0] / abs(vals[0]))
