@@ -626,7 +626,7 @@ def run_precision(args):
       seeds) and integer non-negative matrices (floor(|G| + |G|^T), entries 0..5; a quarter as
       many seeds) against their exact hafnians (the exact sieve over residues, pinned against
       the CPU modular oracle); signed real and complex matrices against the double-double sieve (pinned against the
-      _Float128 oracle to 1e-20 at n <= 20), ``--precision-dd-seeds`` seeds (half that for the
+      _Float128 oracle to the last bits of complex128 at n <= 20), ``--precision-dd-seeds`` seeds (half that for the
       complex class, whose double-double run takes minutes).  Times per hafnian per mode."""
     import numpy as np
 
