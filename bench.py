@@ -3,7 +3,7 @@
 Workload: the plain Glynn hafnian of a 40x40 complex128 symmetric matrix A = (G + G^T)/2,
 Re G, Im G ~ N(0, 1/2) iid, seed 0 (524,288 sieve terms).  One step = one hafnian.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|df] [--impl gb300|reference]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|df|dd] [--impl gb300|reference]
 
 value    : hafnians/s with the input resident in HBM (device time of the sieve + reduction
            launches, CUDA events on the launching stream, L2 flushed between steps), summed
@@ -15,7 +15,13 @@ roofline : algorithmic flops of the sieve (thewalrus_gb300.costmodel) / mean dev
 cpu_baseline : the CPU oracle (a C restatement of the reference algorithm: mixed-radix term
            order, power traces by repeated matrix products) on all host cores, timed on a
            bounded sample of the same hafnian's terms and scaled to hafnians/s.
---impl reference : that CPU restatement alone, as the reference arm (rank 0 only).
+rel_err_vs_reference : the result against the value the reference's own code produced for the
+           same input (committed fixture), and against the long-double oracle.
+batch, serve : (one GPU, default workload) the batched form on a stated subset of the
+           4,096-instance workload and the served form at two arrival rates, each against one
+           call per instance and checked against the oracle (see batch_summary, serve_summary).
+--impl reference : that CPU restatement alone, as the reference arm (rank 0 only), on whole
+           hafnians.
 """
 import argparse
 import json
@@ -385,7 +391,7 @@ def serve_summary(args):
     from thewalrus_gb300.serving import GaussianState, ProbabilityServer, poisson_requests, summary
 
     states = [GaussianState.synthetic(modes=64, seed=s) for s in range(4)]
-    srv = ProbabilityServer(states, precision="fp64", max_batch=256, streams=3)
+    srv = ProbabilityServer(states, precision="fp64", max_batch=256, streams=args.serve_streams)
     srv.serve(poisson_requests(states, 1e6, 16, photons=(8, 16), seed=99))  # warm-up
     rows = []
     err, checked = 0.0, 0
@@ -406,7 +412,7 @@ def serve_summary(args):
                 err = max(err, abs(lhaf - want) / abs(want))
                 checked += 1
     # the same requests at the top rate, admitted oldest first (no cost ordering) for contrast
-    fifo = ProbabilityServer(states, precision="fp64", max_batch=256, streams=3, order="arrival")
+    fifo = ProbabilityServer(states, precision="fp64", max_batch=256, streams=args.serve_streams, order="arrival")
     t0 = time.perf_counter()
     res = fifo.serve(reqs)
     arrival = summary(res, makespan=time.perf_counter() - t0)
@@ -578,7 +584,7 @@ def run_serve(args):
     from thewalrus_gb300.serving import GaussianState, ProbabilityServer, poisson_requests, summary
 
     states = [GaussianState.synthetic(modes=64, seed=s) for s in range(4)]
-    srv = ProbabilityServer(states, precision=args.precision, max_batch=256, streams=3)
+    srv = ProbabilityServer(states, precision=args.precision, max_batch=256, streams=args.serve_streams)
     lo, hi = args.photons
     srv.serve(poisson_requests(states, 1e6, 8, photons=(lo, min(hi, lo + 8)), seed=99))  # warm-up
     rows = []
@@ -759,6 +765,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the batch and serve sub-objects of the default line")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[1000.0, 20000.0])
+    ap.add_argument("--serve-streams", type=int, default=3, help="stream slots of the server")
     ap.add_argument("--workload", choices=["n40", "loop", "batch", "serve", "precision", "sample"], default="n40",
                     help="n40: the benchmark line; the others report the other configurations")
     ap.add_argument("--batch-count", type=int, default=4096)
