@@ -70,3 +70,25 @@ def test_balanced_loop_values():
     got = complex(oracle.loop_haf_prepared(q.A, q.D, q.reps))
     want = complex(oracle.loop_hafnian(A, gamma, [1] * n))
     assert abs(got - want) <= 1e-12 * abs(want)
+
+
+def test_batch_balancing_leaves_the_batch_edges_alone():
+    # a badly scaled fixed part: balancing scales only pairs from `first` on
+    rng = np.random.default_rng(13)
+    B, D, fixed, cutoff = wl.batch_loop_calls(count=1, seed=14, modes=7, cutoff=3)[0]
+    inst = tw.prepare_loop_hafnian_batch(B, D, list(fixed), cutoff)
+    n = inst.A.shape[0]
+    E = n // 2
+    first = 1 if inst.struct.kind == 3 else 2
+    s = np.ldexp(1.0, rng.integers(-30, 30, size=E))
+    s[:first] = 1.0
+    d = np.concatenate([s, 1 / s])
+    Ax, Dx = d[:, None] * inst.A * d[None, :], d * inst.D
+    bal = H._pair_balance(Ax, Dx, first=first)
+    assert bal is not None
+    # the extra scale of vertex i from the diagonal: (d_i s_i)^2 / d_i^2
+    diag = np.abs(np.diagonal(Ax)) > 0
+    k = np.round(0.5 * np.log2(np.abs(np.diagonal(bal[0])[diag] / np.diagonal(Ax)[diag])))
+    idx = np.flatnonzero(diag)
+    fixed_ends = (idx >= first) & ((idx < E) | (idx >= E + first))
+    assert not np.any(k[~fixed_ends]) and np.any(k[fixed_ends])

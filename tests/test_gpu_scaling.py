@@ -107,3 +107,24 @@ def test_small_entry_gaussian_state_loops(n):
     assert rel(tw.hafnian_repeated(B, [1] * n, mu=gamma, loop=True, precision="dd"), want) < RTOL
     want = complex(oracle.hafnian(B, precision="long"))
     assert rel(tw.hafnian(B), want) < RTOL
+
+
+def test_batch_kinds_invariant_under_pair_scaling():
+    """loop_hafnian_batch instances (batch edge first, the odd mode's edge second for odd
+    cutoffs) give the same outputs after a pair scaling of their fixed edges -- what the host's
+    pair balancing relies on for them."""
+    rng = np.random.default_rng(15)
+    for seed, cutoff in ((16, 4), (17, 5)):
+        B, D, fixed, _ = wl.batch_loop_calls(count=1, seed=seed, modes=7, cutoff=cutoff)[0]
+        inst = tw.prepare_loop_hafnian_batch(B, D, list(fixed), cutoff)
+        want = nat.run([inst], "fp64")
+        n = inst.A.shape[0]
+        E = n // 2
+        first = 1 if inst.struct.kind == nat.WG_KIND_BATCH_EVEN else 2
+        s = np.ldexp(1.0, rng.integers(-20, 20, size=E))
+        s[:first] = 1.0
+        d = np.concatenate([s, 1 / s])
+        scaled = nat.Instance(inst.struct.kind, d[:, None] * inst.A * d[None, :], inst.reps, D=d * inst.D,
+                              batch_max=inst.struct.batch_max, cutoff=inst.struct.cutoff)
+        got = nat.run([scaled], "fp64")
+        assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want)), (seed, cutoff)
