@@ -52,7 +52,9 @@ def test_pair_scaled_hafnian(n, kind, decades):
     d, _ = pair_scaling(n, decades, 1000 * n + decades)
     S = d[:, None] * A * d[None, :]
     assert np.max(np.abs(S)) / np.min(np.abs(S)[np.abs(S) > 0]) > 10.0 ** decades
-    want = complex(oracle.hafnian(A, precision="quad"))  # prod(d) = 1
+    # prod(d) = 1; the unscaled sum is well conditioned (cond ~1e2-1e4), so the oracle's double
+    # arithmetic is good to ~1e-13
+    want = complex(oracle.hafnian(A, precision="double"))
     assert rel(tw.hafnian(S, precision="fp64"), want) < RTOL
     assert rel(tw.hafnian(S, precision="df"), want) < 1e-8
 
@@ -65,7 +67,7 @@ def test_pair_scaled_loop_hafnian(n, decades):
     A = wl.complex_symmetric(n, seed=n + decades)
     d, rng = pair_scaling(n, decades, 2000 * n + decades)
     gamma = (rng.normal(size=n) + 1j * rng.normal(size=n)) * 0.5
-    want = complex(oracle.hafnian_repeated(A, [1] * n, mu=gamma, loop=True, precision="quad"))
+    want = complex(oracle.hafnian_repeated(A, [1] * n, mu=gamma, loop=True, precision="double"))
     S = d[:, None] * A * d[None, :]
     got = tw.hafnian_repeated(S, [1] * n, mu=d * gamma, loop=True, precision="fp64")
     assert rel(got, want * np.prod(d)) < RTOL
@@ -96,16 +98,17 @@ def test_small_entry_gaussian_state_loops(n):
     pivots against the rows above (1e-15 after 22 columns), which a deflation test made in that
     frame took for rounding residues -- relative errors of 0.03 at n = 20 up to 760 at n = 28
     before the test moved to the classic frame.  These sums are well conditioned (sum|term| /
-    |sum| ~ 1e2..1e3): 1e-10 against the oracle."""
+    |sum| ~ 1e2..1e3), so the oracle's double arithmetic (the reference algorithm) is good to
+    ~1e-13 and the bar is 1e-10."""
     from thewalrus_gb300.serving import GaussianState
     st = GaussianState.synthetic(modes=64, seed=3)
     rng = np.random.default_rng(n)
     modes = np.sort(rng.choice(64, size=n, replace=False))
     B, gamma = st.B[np.ix_(modes, modes)], st.gamma[modes]
-    want = complex(oracle.hafnian_repeated(B, [1] * n, mu=gamma, loop=True, precision="long"))
+    want = complex(oracle.hafnian_repeated(B, [1] * n, mu=gamma, loop=True, precision="double"))
     assert rel(tw.hafnian_repeated(B, [1] * n, mu=gamma, loop=True), want) < RTOL
     assert rel(tw.hafnian_repeated(B, [1] * n, mu=gamma, loop=True, precision="dd"), want) < RTOL
-    want = complex(oracle.hafnian(B, precision="long"))
+    want = complex(oracle.hafnian(B, precision="double"))
     assert rel(tw.hafnian(B), want) < RTOL
 
 
