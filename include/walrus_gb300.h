@@ -121,7 +121,8 @@ int wg_plan_create(const wg_instance* inst, int count, int precision, double chu
 
 /* Tuning knobs of a plan (zero-initialised fields take the defaults):
  *   chunk_scale       chunks per resident warp relative to the default 4 (term-chunk size)
- *   max_warps_per_cta cap on warps per CTA (default: as many as shared memory allows, <= 8)
+ *   max_warps_per_cta cap on warps per CTA (default 7; at most 8: as many as shared memory
+ *                     allows up to the cap)
  *   merge_classes     1: one persistent launch per scalar type instead of per occupancy class
  *   use_graph         1: wg_plan_execute captures its launches into a CUDA graph on first use
  *                        and replays the graph afterwards

@@ -81,6 +81,12 @@ static inline cudaError_t sieve_tables_all(const double* binom, const double* in
   return e;
 }
 
+// Default cap on warps per CTA.  Seven measured faster than eight where eight fit in one SM's
+// shared memory: complex FP64 n = 40 247.9 ms against 249.7 ms, n = 36 49.07 against 49.79 ms,
+// double-float n = 40 135.6 against 136.6 ms; six gives the same as seven, and n = 32, 42 and
+// the real kernels (several CTAs per SM) are unchanged.
+constexpr int kDefaultWarpsPerCta = 7;
+
 // Launch shape for a per-warp workspace of `bytes`: warps per CTA (at most wpc_cap) for the most
 // resident warps per SM -- shared memory and registers decide how many CTAs fit -- larger CTAs
 // on ties, e.g. 2 CTAs x 7 warps where 1 x 8 would leave room unused.  Returns {wpc, CTAs per

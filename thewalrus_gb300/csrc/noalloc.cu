@@ -202,7 +202,7 @@ extern "C" int wg_hafnian_noalloc(const void* A_dev, int n, int dtype, const int
   const WarpLayout L = make_layout(st, m_max, m_max, std::min(d.K, m_max), d.K + 2, 2,
                                    all_odd && d.K < m_max);
   // the same launch shape as wg_hafnian's for this workspace
-  const std::pair<int, int> sh = best_shape(st, L.bytes, 8);
+  const std::pair<int, int> sh = best_shape(st, L.bytes, kDefaultWarpsPerCta);
   const int wpc = sh.first, per_sm = sh.second;
   if (wpc < 1) return err(WG_EINVAL, "size beyond the maximum: per-warp workspace does not fit");
   if (per_sm < 1) return err(WG_ECUDA, "sieve kernel cannot be resident");

@@ -584,7 +584,7 @@ static int finalize_plan(std::vector<Prepared>& P, int precision, const wg_plan_
                          GatherSpec* gs) {
   const int count = (int)P.size();
   const double chunk_scale = opt.chunk_scale > 0 ? opt.chunk_scale : 1.0;
-  const int wpc_cap = opt.max_warps_per_cta > 0 ? std::min(opt.max_warps_per_cta, 8) : 8;
+  const int wpc_cap = opt.max_warps_per_cta > 0 ? std::min(opt.max_warps_per_cta, 8) : kDefaultWarpsPerCta;
   pl->use_graph = opt.use_graph != 0;
   pl->serial_groups = opt.serial_groups != 0;
   pl->precision = precision;
