@@ -81,10 +81,11 @@ static inline cudaError_t sieve_tables_all(const double* binom, const double* in
   return e;
 }
 
-// Default cap on warps per CTA.  Seven measured faster than eight where eight fit in one SM's
-// shared memory: complex FP64 n = 40 247.9 ms against 249.7 ms, n = 36 49.07 against 49.79 ms,
-// double-float n = 40 135.6 against 136.6 ms; six gives the same as seven, and n = 32, 42 and
-// the real kernels (several CTAs per SM) are unchanged.
+// Default cap on warps per CTA.  Below 8 the shape search below takes two CTAs of 4 warps where
+// one CTA of 8 would fit (the same 8 warps per SM), and that measured faster: complex FP64
+// n = 40 247.9 ms against 249.7 ms, n = 36 49.07 against 49.79 ms, double-float n = 40 135.6
+// against 136.6 ms; a cap of 6 gives the same as 7, and n = 32, 42 and the real kernels (several
+// CTAs per SM already) are unchanged.
 constexpr int kDefaultWarpsPerCta = 7;
 
 // Launch shape for a per-warp workspace of `bytes`: warps per CTA (at most wpc_cap) for the most
