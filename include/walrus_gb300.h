@@ -202,7 +202,11 @@ int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
  * IEEE and exact references (no counterpart in the reference): op 0 the pivot reciprocal 1/x
  * (approximate reciprocal + two Newton steps), 1 the double-double reciprocal of (x, x_lo), 2 the
  * double-double quotient (x, x_lo) / k with k = (int)y, 3 the double-double product of (x, x_lo)
- * and (y, y_lo).  in: 4 doubles per element (x, x_lo, y, y_lo); out: 2 per element (hi, lo). */
+ * and (y, y_lo), 4 the double-float reciprocal of (x, x_lo), 5 the complex double-float
+ * reciprocal of (x, x_lo) + i (y, y_lo) (out: its real and imaginary parts, each hi + lo in FP64),
+ * 6 the double-float quotient (x, x_lo) / k with k = (int)y; double-float inputs are the float
+ * parts, given as doubles.  in: 4 doubles per element (x, x_lo, y, y_lo); out: 2 per element
+ * (hi, lo). */
 int wg_check_arith(int op, const double* in, int n, double* out);
 
 /* Allocation-free plain hafnian (FP64 terms).  No counterpart in the reference: it exists for

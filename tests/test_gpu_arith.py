@@ -7,6 +7,11 @@ references.
 * The double-double primitives (reciprocal, division by a small integer, product) against exact
   rational arithmetic: relative error below 2^-100 (a double-double carries 106 bits; the
   primitives give up a few bits to their final renormalisation).
+* The double-float pivot reciprocal (real and complex, FP32 instructions only: a power-of-two
+  prescaling, the float reciprocal and one Newton correction) and the division by a small integer
+  of the series, against exact rationals: relative error below 2^-44 (a double-float carries 48
+  bits) for operands and results within 2^+-90, where the low part of a double-float is still a
+  normal float (below ~2^-100 it loses bits to underflow, in any double-float arithmetic).
 """
 from fractions import Fraction
 
@@ -62,3 +67,38 @@ def test_double_double_product():
     worst = max(_rel(p, q, (Fraction(float(a)) + Fraction(float(b))) * (Fraction(float(c)) + Fraction(float(d))))
                 for p, q, a, b, c, d in zip(ph, pl, ah, al, bh, bl))
     assert worst < 2.0 ** -100, worst
+
+
+def _df_inputs(rng, count, lo_exp=-90, hi_exp=90):
+    hi = np.ldexp(rng.uniform(1.0, 2.0, size=count), rng.integers(lo_exp, hi_exp, size=count))
+    hi = (hi * rng.choice([-1.0, 1.0], size=count)).astype(np.float32).astype(np.float64)
+    lo = (hi * rng.uniform(-1.0, 1.0, size=count) * 2.0 ** -25).astype(np.float32).astype(np.float64)
+    return hi, lo
+
+
+def test_double_float_reciprocals_and_division():
+    rng = np.random.default_rng(4)
+    hi, lo = _df_inputs(rng, 400)
+    hi = np.concatenate([hi, [1.0, -1.0, 3.0, 0.1, 2.0 ** -90, 2.0 ** 90, 1.5 * 2.0 ** 89]]).astype(np.float32).astype(np.float64)
+    lo = np.concatenate([lo, np.zeros(7)])
+    rh, rl = nat.check_arith(4, hi, lo)
+    worst = max(_rel(a, b, 1 / (Fraction(float(h)) + Fraction(float(l)))) for a, b, h, l in zip(rh, rl, hi, lo))
+    assert worst < 2.0 ** -44, worst
+    # complex: re and im of 1 / z, z = (hi, lo) + i (yh, yl), over mixed magnitudes of the parts
+    yh, yl = _df_inputs(rng, 407, -20, 20)
+    yh[::5] = 0.0
+    yl[::5] = 0.0
+    re, im = nat.check_arith(5, hi[:407], lo[:407], yh, yl)
+    for k in range(407):
+        x = Fraction(float(hi[k])) + Fraction(float(lo[k]))
+        y = Fraction(float(yh[k])) + Fraction(float(yl[k]))
+        d = x * x + y * y
+        ex, ey = x / d, -y / d
+        scale = max(abs(ex), abs(ey))
+        assert abs(Fraction(float(re[k])) - ex) / scale < 2.0 ** -44, (k, float(re[k]), float(ex))
+        assert abs(Fraction(float(im[k])) - ey) / scale < 2.0 ** -44, (k, float(im[k]), float(ey))
+    k = rng.integers(1, 250, size=407).astype(np.float64)
+    qh, ql = nat.check_arith(6, hi[:407], lo[:407], k)
+    worst = max(_rel(a, b, (Fraction(float(h)) + Fraction(float(l))) / int(kk))
+                for a, b, h, l, kk in zip(qh, ql, hi, lo, k))
+    assert worst < 2.0 ** -44, worst

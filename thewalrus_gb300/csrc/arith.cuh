@@ -115,6 +115,45 @@ __device__ __forceinline__ dfr df_fma2(dfr a, dfr b, dfr d, dfr f, dfr c) {
   float lo = (s1.lo + s2.lo) + (c.lo + (e1 + e2));
   return df_fast_two_sum(s2.hi, lo);
 }
+// a * s for a float s that is exact (the small integers and halves of the series and the gather)
+__device__ __forceinline__ dfr df_mul_f(dfr a, float s) {
+  float p = a.hi * s;
+  float e = fmaf(a.hi, s, -p);
+  e = fmaf(a.lo, s, e);
+  return df_fast_two_sum(p, e);
+}
+// a / k for a small positive integer k: an approximate float quotient q1, whose remainder
+// a.hi - q1 k is exact in one FMA (it is a multiple of ulp(q1) of a few bits), and the quotient
+// of the remainder as the low part
+__device__ __forceinline__ dfr df_div_int(dfr a, int k) {
+  const float kf = (float)k;
+  const float q1 = __fdividef(a.hi, kf);
+  const float r = fmaf(neg_f(q1), kf, a.hi) + a.lo;
+  return df_fast_two_sum(q1, __fdividef(r, kf));
+}
+// 2^-e for a float whose magnitude bits are `bits` and |x| in [2^e, 2^(e+1)), e clamped to the
+// normal range: multiplying by it is exact and brings |x| into [1, 2)
+__device__ __forceinline__ float df_pow2_inv(unsigned bits) {
+  int ef = 254 - (int)(bits >> 23);
+  ef = ef < 1 ? 1 : (ef > 254 ? 254 : ef);
+  return __int_as_float(ef << 23);
+}
+// 1/a for |a.hi| in [1, 8): the float reciprocal r0 and Newton's correction in double-float,
+// r = r0 (1 + e + e^2) with e = 1 - a r0 (the first product exact in one FMA): relative error
+// ~2^-47, FP32 instructions only
+__device__ __forceinline__ dfr df_recip_unit(dfr a) {
+  const float r0 = __frcp_rn(a.hi);
+  float e = fmaf(neg_f(a.hi), r0, 1.0f);
+  e = fmaf(neg_f(a.lo), r0, e);
+  return df_fast_two_sum(r0, r0 * fmaf(e, e, e));
+}
+// 1/a: scaled by a power of two into [1, 2), inverted, scaled back (exact unless the result
+// leaves float's normal range)
+__device__ __forceinline__ dfr df_recip(dfr a) {
+  const float f = df_pow2_inv(absbits_f(a.hi));
+  const dfr r = df_recip_unit({a.hi * f, a.lo * f});
+  return {r.hi * f, r.lo * f};
+}
 __device__ __forceinline__ double df_to_d(dfr a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ dfr df_from_d(double x) {
   float h = __double2float_rn(x);
@@ -224,6 +263,7 @@ struct Ar<double> {
   __device__ static __forceinline__ S neg(S a) { return neg_d(a); }
   __device__ static __forceinline__ S conj(S a) { return a; }
   __device__ static __forceinline__ S scale(S a, double s) { return a * s; }
+  __device__ static __forceinline__ S scale_f(S a, float s) { return a * (double)s; }
   __device__ static __forceinline__ S from_c64(c64 v) { return v.re; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {a, 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_d(a); }
@@ -266,6 +306,7 @@ struct Ar<c64> {
   __device__ static __forceinline__ S neg(S a) { return {neg_d(a.re), neg_d(a.im)}; }
   __device__ static __forceinline__ S conj(S a) { return {a.re, neg_d(a.im)}; }
   __device__ static __forceinline__ S scale(S a, double s) { return {a.re * s, a.im * s}; }
+  __device__ static __forceinline__ S scale_f(S a, float s) { return scale(a, (double)s); }
   __device__ static __forceinline__ S from_c64(c64 v) { return v; }
   __device__ static __forceinline__ c64 to_c64(S a) { return a; }
   __device__ static __forceinline__ unsigned long long key(S a) {
@@ -309,13 +350,15 @@ struct Ar<dfr> {
   __device__ static __forceinline__ S neg(S a) { return df_neg(a); }
   __device__ static __forceinline__ S conj(S a) { return a; }
   __device__ static __forceinline__ S scale(S a, double s) { return df_mul(a, df_from_d(s)); }
+  __device__ static __forceinline__ S scale_f(S a, float s) { return df_mul_f(a, s); }
+  __device__ static __forceinline__ S div_int(S a, int k) { return df_div_int(a, k); }
   __device__ static __forceinline__ S from_c64(c64 v) { return df_from_d(v.re); }
   __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a), 0.0}; }
   __device__ static __forceinline__ unsigned long long key(S a) { return absbits_f(a.hi); }
   __device__ static __forceinline__ unsigned long long key_deflate(unsigned long long k) { return key_shift_f(k); }
   __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)k; }
   __device__ static __forceinline__ bool is_zero(S a) { return absbits_f(a.hi) == 0; }
-  __device__ static __forceinline__ S recip(S a) { return df_from_d(1.0 / df_to_d(a)); }
+  __device__ static __forceinline__ S recip(S a) { return df_recip(a); }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return a; }
   __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) { a = v; }
   __device__ static __forceinline__ Comp cadd(Comp a, Comp b) { return df_add(a, b); }
@@ -356,6 +399,8 @@ struct Ar<cdf> {
     dfr t = df_from_d(s);
     return {df_mul(a.re, t), df_mul(a.im, t)};
   }
+  __device__ static __forceinline__ S scale_f(S a, float s) { return {df_mul_f(a.re, s), df_mul_f(a.im, s)}; }
+  __device__ static __forceinline__ S div_int(S a, int k) { return {df_div_int(a.re, k), df_div_int(a.im, k)}; }
   __device__ static __forceinline__ S from_c64(c64 v) { return {df_from_d(v.re), df_from_d(v.im)}; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {df_to_d(a.re), df_to_d(a.im)}; }
   __device__ static __forceinline__ unsigned long long key(S a) {
@@ -366,9 +411,14 @@ struct Ar<cdf> {
   __device__ static __forceinline__ unsigned key32(unsigned long long k) { return (unsigned)k; }
   __device__ static __forceinline__ bool is_zero(S a) { return (absbits_f(a.re.hi) | absbits_f(a.im.hi)) == 0; }
   __device__ static __forceinline__ S recip(S a) {
-    c64 z = to_c64(a);
-    double d = 1.0 / ::fma(z.re, z.re, z.im * z.im);
-    return from_c64({z.re * d, -z.im * d});
+    // conj(z) / |z|^2 on z scaled by a power of two into [1, 2) (so |z|^2 in [1, 8) neither
+    // overflows nor underflows), in FP32 instructions only
+    const unsigned x = absbits_f(a.re.hi), y = absbits_f(a.im.hi);
+    const float f = df_pow2_inv(x > y ? x : y);
+    const dfr re = {a.re.hi * f, a.re.lo * f}, im = {a.im.hi * f, a.im.lo * f};
+    const dfr d = df_recip_unit(df_fma2(re, re, im, im, dfr{0.f, 0.f}));
+    const dfr rr = df_mul(re, d), ri = df_mul(im, d);
+    return {{rr.hi * f, rr.lo * f}, {neg_f(ri.hi * f), neg_f(ri.lo * f)}};
   }
   __device__ static __forceinline__ Comp comp(const S& a, int i) { return i ? a.im : a.re; }
   __device__ static __forceinline__ void set_comp(S& a, int i, Comp v) {
@@ -406,6 +456,7 @@ struct Ar<ddr> {
   __device__ static __forceinline__ S neg(S a) { return dd_neg(a); }
   __device__ static __forceinline__ S conj(S a) { return a; }
   __device__ static __forceinline__ S scale(S a, double s) { return dd_mul_d(a, s); }
+  __device__ static __forceinline__ S scale_f(S a, float s) { return dd_mul_d(a, (double)s); }
   __device__ static __forceinline__ S div_int(S a, int k) { return dd_div_int(a, k); }
   __device__ static __forceinline__ S from_c64(c64 v) { return {v.re, 0.0}; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {a.hi, 0.0}; }
@@ -452,6 +503,7 @@ struct Ar<cdd> {
   __device__ static __forceinline__ S neg(S a) { return {dd_neg(a.re), dd_neg(a.im)}; }
   __device__ static __forceinline__ S conj(S a) { return {a.re, dd_neg(a.im)}; }
   __device__ static __forceinline__ S scale(S a, double s) { return {dd_mul_d(a.re, s), dd_mul_d(a.im, s)}; }
+  __device__ static __forceinline__ S scale_f(S a, float s) { return scale(a, (double)s); }
   __device__ static __forceinline__ S div_int(S a, int k) { return {dd_div_int(a.re, k), dd_div_int(a.im, k)}; }
   __device__ static __forceinline__ S from_c64(c64 v) { return {{v.re, 0.0}, {v.im, 0.0}}; }
   __device__ static __forceinline__ c64 to_c64(S a) { return {a.re.hi, a.im.hi}; }

@@ -1253,14 +1253,29 @@ static __global__ void arith_check_kernel(int op, const double* __restrict__ in,
     case 0: r.hi = recip_newton(x); break;
     case 1: r = dd_recip({x, xl}); break;
     case 2: r = dd_div_int({x, xl}, (int)y); break;
-    default: r = dd_mul({x, xl}, {y, yl}); break;
+    case 3: r = dd_mul({x, xl}, {y, yl}); break;
+    case 4: {  // double-float reciprocal (inputs: the float parts)
+      const dfr q = Ar<dfr>::recip({(float)x, (float)xl});
+      r = {(double)q.hi, (double)q.lo};
+      break;
+    }
+    case 5: {  // complex double-float reciprocal: out = (re, im), each part's hi + lo in FP64
+      const cdf q = Ar<cdf>::recip({{(float)x, (float)xl}, {(float)y, (float)yl}});
+      r = {df_to_d(q.re), df_to_d(q.im)};
+      break;
+    }
+    default: {  // double-float division by a small integer
+      const dfr q = df_div_int({(float)x, (float)xl}, (int)y);
+      r = {(double)q.hi, (double)q.lo};
+      break;
+    }
   }
   out[2 * i] = r.hi;
   out[2 * i + 1] = r.lo;
 }
 
 int wg_check_arith(int op, const double* in, int n, double* out) {
-  if (op < 0 || op > 3 || n < 0 || (n > 0 && (!in || !out))) return fail(WG_EINVAL, "bad arithmetic check arguments");
+  if (op < 0 || op > 6 || n < 0 || (n > 0 && (!in || !out))) return fail(WG_EINVAL, "bad arithmetic check arguments");
   if (n == 0) return WG_OK;
   int rc = ensure_init(-1);
   if (rc) return rc;

@@ -142,7 +142,7 @@ template <class S>
 __device__ __forceinline__ S half_of(S x) {
   using A = Ar<S>;
   if constexpr (A::modular) return A::mul(x, A::half());
-  else return A::scale(x, 0.5);
+  else return A::scale_f(x, 0.5f);
 }
 
 template <class S>
@@ -151,7 +151,7 @@ __device__ __forceinline__ S scale_int(S x, int d) {
   if (d == 1) return x;
   if (d == -1) return A::neg(x);
   if constexpr (A::modular) return A::mul(x, A::of_int(d));
-  else return A::scale(x, (double)d);
+  else return A::scale_f(x, (float)d);  // |d| is a small repetition count: exact in float
 }
 
 template <class S>
@@ -532,16 +532,20 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
         const int l0 = sc.len[0], l1 = sc.len[1], l2 = sc.len[2];
         const int tot = l0 + l1 + l2;
         S acc = A::zero();
-        if (A::fp64 && tile && i >= Kc + 3 && rc0 == Kc - 1 && rc1 == Kc - 1) {
+        if ((A::fp64 || A::cplx) && tile && i >= Kc + 3 && rc0 == Kc - 1 && rc1 == Kc - 1) {
           // steady state of the tile form: every c[i+row-r-1] read lives in the tile and no
           // subdiagonal zero truncates the sums, so along a piece both operands step linearly --
-          // T_r = W[wi+row-r][wi+row] by -ldw, c[i+row-r-1][j-r-1] = W[j-r-1][nb+i+row-r-4] by
-          // -(ldw+1) -- and an iteration is two loads and one multiply-add
+          // T_r = W[wi+row-r][wi+row] by -ldw (normalised forms; complex double-float reads its
+          // products tb[row kw + r] by +1), c[i+row-r-1][j-r-1] = W[j-r-1][nb+i+row-r-4] by
+          // -(ldw+1) -- and an iteration is two loads and one multiply-add.  (Real double-float
+          // measured 3 % slower in this form than in the general loop below: it keeps that.)
+          const S* __restrict__ Tsrc = A::fp64 ? W : tb;
+          const int sT = A::fp64 ? -ldw : 1;
           int oT[3], oC[3];
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
             const int row = (sc.rowmask >> q) & 1, jq = sc.j[q], r0 = sc.rlo[q];
-            oT[q] = (wi + row - r0) * ldw + wi + row;
+            oT[q] = A::fp64 ? (wi + row - r0) * ldw + wi + row : row * kw + r0;
             oC[q] = (jq - r0 - 1) * ldw + nb + i + row - r0 - 4;
           }
           int q = 0, left = l0, pT = oT[0], pC = oC[0];
@@ -554,8 +558,8 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
               pT = q == 1 ? oT[1] : oT[2];
               pC = q == 1 ? oC[1] : oC[2];
             }
-            acc = A::fma(W[pT], W[pC], acc);
-            pT -= ldw;
+            acc = A::fma(Tsrc[pT], W[pC], acc);
+            pT += sT;
             pC -= ldw + 1;
             --left;
           }
@@ -678,11 +682,11 @@ __device__ void inv_sqrt_series(const S* __restrict__ cpoly, int Kc, S* __restri
         acc = A::fma(cpoly[n - k], A::mul(gk, A::mul(A::of_int(n + k), A::half())), g[n]);
         if (n == k + 1) acc = A::neg(A::mul(acc, inv_of<S>(n)));
       } else {
-        acc = A::fma(cpoly[n - k], A::scale(gk, 0.5 * (double)(n + k)), g[n]);
-        if constexpr (A::dd) {  // 1/n to the type's precision
-          if (n == k + 1) acc = A::neg(A::div_int(acc, n));
-        } else {
+        acc = A::fma(cpoly[n - k], A::scale_f(gk, 0.5f * (float)(n + k)), g[n]);
+        if constexpr (A::fp64 && !A::dd) {
           if (n == k + 1) acc = A::scale(acc, -inv_int(n));
+        } else {  // 1/n to the type's precision, in its own instructions
+          if (n == k + 1) acc = A::neg(A::div_int(acc, n));
         }
       }
       g[n] = acc;
@@ -708,11 +712,11 @@ __device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, in
         acc = A::fma(A::mul(q[n - k], A::of_int(n - k)), ek, e[n]);
         if (n == k + 1) acc = A::mul(acc, inv_of<S>(n));
       } else {
-        acc = A::fma(A::scale(q[n - k], (double)(n - k)), ek, e[n]);
-        if constexpr (A::dd) {
-          if (n == k + 1) acc = A::div_int(acc, n);
-        } else {
+        acc = A::fma(A::scale_f(q[n - k], (float)(n - k)), ek, e[n]);
+        if constexpr (A::fp64 && !A::dd) {
           if (n == k + 1) acc = A::scale(acc, inv_int(n));
+        } else {
+          if (n == k + 1) acc = A::div_int(acc, n);
         }
       }
       e[n] = acc;
