@@ -268,30 +268,30 @@ __device__ __forceinline__ void phase_b_split(S* __restrict__ W, const S* __rest
     const int s = vi / A::NC, part = vi % A::NC;
     const int a = base + r8 + 8 * s;
     if (!h2 && (NCOMP == 2 || !h1) && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z;
-    return;
-  }
-  Comp u[NCP / 2];
+  } else {
+    Comp u[NCP / 2];
 #pragma unroll
-  for (int i = 0; i < NCP / 2; ++i) {
-    Comp send = h1 ? v[i] : v[NCP / 2 + i];
-    Comp keep = h1 ? v[NCP / 2 + i] : v[i];
-    u[i] = A::cadd(keep, A::shfl_xor(send, 16));
-  }
-  Comp z[NCP / 4];
+    for (int i = 0; i < NCP / 2; ++i) {
+      Comp send = h1 ? v[i] : v[NCP / 2 + i];
+      Comp keep = h1 ? v[NCP / 2 + i] : v[i];
+      u[i] = A::cadd(keep, A::shfl_xor(send, 16));
+    }
+    Comp z[NCP / 4];
 #pragma unroll
-  for (int i = 0; i < NCP / 4; ++i) {
-    Comp send = h2 ? u[i] : u[NCP / 4 + i];
-    Comp keep = h2 ? u[NCP / 4 + i] : u[i];
-    z[i] = A::cadd(keep, A::shfl_xor(send, 8));
-  }
-  __syncwarp();
-  const int off = (h1 ? NCP / 2 : 0) + (h2 ? NCP / 4 : 0);
+    for (int i = 0; i < NCP / 4; ++i) {
+      Comp send = h2 ? u[i] : u[NCP / 4 + i];
+      Comp keep = h2 ? u[NCP / 4 + i] : u[i];
+      z[i] = A::cadd(keep, A::shfl_xor(send, 8));
+    }
+    __syncwarp();
+    const int off = (h1 ? NCP / 2 : 0) + (h2 ? NCP / 4 : 0);
 #pragma unroll
-  for (int i = 0; i < NCP / 4; ++i) {
-    const int vi = off + i;
-    const int s = vi / A::NC, part = vi % A::NC;
-    const int a = base + r8 + 8 * s;
-    if (vi < NCOMP && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
+    for (int i = 0; i < NCP / 4; ++i) {
+      const int vi = off + i;
+      const int s = vi / A::NC, part = vi % A::NC;
+      const int a = base + r8 + 8 * s;
+      if (vi < NCOMP && a < rows) reinterpret_cast<Comp*>(&W[a * ldw + j + 1])[part] = z[i];
+    }
   }
 }
 
