@@ -160,7 +160,9 @@ int wg_plan_chunk(const wg_plan* plan, int chunk, int* inst, int* part, long lon
 /* Bytes moved by wg_plan_create (host to device) and by wg_plan_read (device to host). */
 int wg_plan_transfer_bytes(const wg_plan* plan, long long* h2d, long long* d2h);
 int wg_plan_destroy(wg_plan* plan);
-/* create + execute + read + destroy */
+/* create + execute + read + destroy, stream-ordered on `stream` (NULL: the calling thread's
+ * default stream, cudaStreamPerThread): the plan's memory comes from the device's default
+ * stream-ordered pool, which keeps up to 256 MiB of freed memory for the next call. */
 int wg_run(const wg_instance* inst, int count, int precision, double* out, void* stream);
 
 /* Serving: a Gaussian state resident on the device and plans whose loop-hafnian matrices are

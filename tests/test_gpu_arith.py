@@ -8,10 +8,13 @@ references.
   rational arithmetic: relative error below 2^-100 (a double-double carries 106 bits; the
   primitives give up a few bits to their final renormalisation).
 * The double-float pivot reciprocal (real and complex, FP32 instructions only: a power-of-two
-  prescaling, the float reciprocal and one Newton correction) and the division by a small integer
-  of the series, against exact rationals: relative error below 2^-44 (a double-float carries 48
-  bits) for operands and results within 2^+-90, where the low part of a double-float is still a
-  normal float (below ~2^-100 it loses bits to underflow, in any double-float arithmetic).
+  prescaling, the float reciprocal and its Newton series with the residual kept in double-float)
+  against exact rationals: real within 2^-48 (emulated worst case 2^-49: as accurate as rounding
+  an FP64 reciprocal), complex within 2^-45 (emulated worst case 2^-45.9: |z|^2 and the two
+  products add their roundings);
+  the division by a small integer of the series within 2^-46; for operands and results within
+  2^+-90, where the low part of a double-float is still a normal float (below ~2^-100 it loses
+  bits to underflow, in any double-float arithmetic).
 """
 from fractions import Fraction
 
@@ -83,7 +86,7 @@ def test_double_float_reciprocals_and_division():
     lo = np.concatenate([lo, np.zeros(7)])
     rh, rl = nat.check_arith(4, hi, lo)
     worst = max(_rel(a, b, 1 / (Fraction(float(h)) + Fraction(float(l)))) for a, b, h, l in zip(rh, rl, hi, lo))
-    assert worst < 2.0 ** -44, worst
+    assert worst < 2.0 ** -48, worst
     # complex: re and im of 1 / z, z = (hi, lo) + i (yh, yl), over mixed magnitudes of the parts
     yh, yl = _df_inputs(rng, 407, -20, 20)
     yh[::5] = 0.0
@@ -95,10 +98,10 @@ def test_double_float_reciprocals_and_division():
         d = x * x + y * y
         ex, ey = x / d, -y / d
         scale = max(abs(ex), abs(ey))
-        assert abs(Fraction(float(re[k])) - ex) / scale < 2.0 ** -44, (k, float(re[k]), float(ex))
-        assert abs(Fraction(float(im[k])) - ey) / scale < 2.0 ** -44, (k, float(im[k]), float(ey))
+        assert abs(Fraction(float(re[k])) - ex) / scale < 2.0 ** -45, (k, float(re[k]), float(ex))
+        assert abs(Fraction(float(im[k])) - ey) / scale < 2.0 ** -45, (k, float(im[k]), float(ey))
     k = rng.integers(1, 250, size=407).astype(np.float64)
     qh, ql = nat.check_arith(6, hi[:407], lo[:407], k)
     worst = max(_rel(a, b, (Fraction(float(h)) + Fraction(float(l))) / int(kk))
                 for a, b, h, l, kk in zip(qh, ql, hi, lo, k))
-    assert worst < 2.0 ** -44, worst
+    assert worst < 2.0 ** -46, worst

@@ -5,9 +5,12 @@ reference's own code produced for the same inputs (``tests/golden/metric_cases.n
 by ``make_golden.py --metric``, which also stores the oracle's long-double values, the sieve
 sum's condition number cond = sum|term| / |sum| and, where cond is large, the _Float128 value).
 
-Tolerances.  The plain hafnians are well conditioned (cond ~7e4 complex): 1e-10 relative for
-FP64 against both the reference and the oracle; 1e-9 for double-float terms, whose 48-bit
-significand meets the complex sieve's cancellation (measured deviation from FP64: 1.2e-10).
+Tolerances.  The plain hafnians are well conditioned (cond 6.8e4 complex, 2.0e5 real): 1e-10
+relative for FP64 against both the reference and the oracle.  Double-float terms carry a 48-bit
+significand, so the sieve's cancellation leaves ~cond x 2^-48 (5e-10 complex, 1.4e-9 real);
+they are held to 16 x cond x 2^-48, the bound ``hafnian_with_error`` states (measured: 1e-10
+complex, 1.2e-9 real; a change in the order of any rounding moves the real one by up to ~10x
+either way within that bound).
 The 40-photon loop hafnian is not: its 110,592 terms cancel to 1 part in cond = 3.4e10, so
 per-term rounding of 2^-53 can move the result by up to 3.8e-6 relative -- the reference's own
 double result is 4.5e-8 from the _Float128 value.  FP64 is held to eps * cond against the
@@ -24,8 +27,8 @@ pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 RTOL = 1e-10
-RTOL_DF = 1e-9
 EPS = 2.0 ** -53
+EPS_DF = 2.0 ** -48
 
 
 @pytest.fixture(scope="module")
@@ -43,9 +46,10 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize("case", ["haf40_complex", "haf40_real"])
-@pytest.mark.parametrize("precision,tol", [("fp64", RTOL), ("df", RTOL_DF)])
-def test_plain_n40_vs_reference(metric, case, precision, tol):
+@pytest.mark.parametrize("precision", ["fp64", "df"])
+def test_plain_n40_vs_reference(metric, case, precision):
     c = metric[case]
+    tol = RTOL if precision == "fp64" else 16 * float(c["cond"]) * EPS_DF
     got = tw.hafnian(c["A"], precision=precision)
     assert isinstance(got, np.complex128)
     assert rel(got, c["out"]) < tol, (case, precision, got, complex(c["out"]))

@@ -9,7 +9,9 @@ Per sieve term with an m x m term matrix (mb = m + border, rows = mb + odd-mode 
 * La Budde's recurrence truncated to Kc = min(K, m) coefficients:
     sum_{i=1..m} sum_{j=1..min(i,Kc)} min(j, i)
 * det^(-1/2) series to degree K: sum_{n=1..K} min(n, Kc)
-* loop variants: Krylov sum_{t=1..K} (t*min(t,m) + 2*t) and exp series K^2/2 (+ N^2/2 odd)
+* loop variants: the border series from La Budde's trailing determinants, per bordered row
+  (1 + odd-mode rows) sum_{t=1..K} (min(t, Kc) + min(t-1, Kc)) (numerator, division by P), and
+  the exp series K^2/2 (+ N^2/2 odd)
 
 ``reference_term_macs`` is the reference's own per-term work (charpoly.powertrace by repeated
 matrix products, (K-1) * m^3 MACs), reported beside, never mixed into, the roofline.
@@ -34,7 +36,7 @@ def term_macs(m, K, border=0, extra_rows=0, loop=False, odd_N=0):
     ser = sum(min(n, Kc) for n in range(1, K + 1))
     extra = 0
     if loop:
-        extra += sum(t * min(t, m) + 2 * t for t in range(1, K + 1)) + K * K // 2
+        extra += (1 + extra_rows) * sum(min(t, Kc) + min(t - 1, Kc) for t in range(1, K + 1)) + K * K // 2
         if odd_N:
             extra += odd_N * odd_N // 2
     return hess + lab + ser + extra

@@ -122,14 +122,14 @@ __device__ __forceinline__ dfr df_mul_f(dfr a, float s) {
   e = fmaf(a.lo, s, e);
   return df_fast_two_sum(p, e);
 }
-// a / k for a small positive integer k: an approximate float quotient q1, whose remainder
-// a.hi - q1 k is exact in one FMA (it is a multiple of ulp(q1) of a few bits), and the quotient
-// of the remainder as the low part
+// a / k for a small positive integer k: the correctly rounded float quotient q1, whose remainder
+// a.hi - q1 k is exact in one FMA (a multiple of ulp(q1) of a few bits), and the quotient of
+// the remainder plus a.lo as the low part (|q2| <= ulp(q1), so its rounding is ~2^-48 of a / k)
 __device__ __forceinline__ dfr df_div_int(dfr a, int k) {
   const float kf = (float)k;
-  const float q1 = __fdividef(a.hi, kf);
+  const float q1 = __fdiv_rn(a.hi, kf);
   const float r = fmaf(neg_f(q1), kf, a.hi) + a.lo;
-  return df_fast_two_sum(q1, __fdividef(r, kf));
+  return df_fast_two_sum(q1, __fdiv_rn(r, kf));
 }
 // 2^-e for a float whose magnitude bits are `bits` and |x| in [2^e, 2^(e+1)), e clamped to the
 // normal range: multiplying by it is exact and brings |x| into [1, 2)
@@ -138,14 +138,23 @@ __device__ __forceinline__ float df_pow2_inv(unsigned bits) {
   ef = ef < 1 ? 1 : (ef > 254 ? 254 : ef);
   return __int_as_float(ef << 23);
 }
-// 1/a for |a.hi| in [1, 8): the float reciprocal r0 and Newton's correction in double-float,
-// r = r0 (1 + e + e^2) with e = 1 - a r0 (the first product exact in one FMA): relative error
-// ~2^-47, FP32 instructions only
+// 1/a for |a.hi| in [1, 8), FP32 instructions only: the correctly rounded float reciprocal r0
+// and 1/a = r0 (1 + e + e^2 + ..) with e = 1 - a r0 = e0 - a.lo r0 (e0 = 1 - a.hi r0 exact in
+// one FMA, the second product split exactly by another), kept as a double-float so that the
+// correction r0 e is formed to ~2^-49; |e| <= 2^-23, so e^2 is the last term that counts.
+// Relative error ~2^-49, as good as rounding the FP64 reciprocal: the pivot reciprocal's error
+// is the same for every multiplier of a column, so it is kept well below the other roundings.
 __device__ __forceinline__ dfr df_recip_unit(dfr a) {
   const float r0 = __frcp_rn(a.hi);
-  float e = fmaf(neg_f(a.hi), r0, 1.0f);
-  e = fmaf(neg_f(a.lo), r0, e);
-  return df_fast_two_sum(r0, r0 * fmaf(e, e, e));
+  const float e0 = fmaf(neg_f(a.hi), r0, 1.0f);
+  const float e1 = neg_f(a.lo) * r0;
+  const float e1l = fmaf(neg_f(a.lo), r0, neg_f(e1));
+  dfr e = df_two_sum(e0, e1);
+  e.lo += e1l;
+  const float ch = r0 * e.hi;
+  const float cl = fmaf(r0, e.hi, neg_f(ch)) + r0 * fmaf(e.hi, e.hi, e.lo);
+  const dfr s = df_fast_two_sum(r0, ch);
+  return df_fast_two_sum(s.hi, s.lo + cl);
 }
 // 1/a: scaled by a power of two into [1, 2), inverted, scaled back (exact unless the result
 // leaves float's normal range)

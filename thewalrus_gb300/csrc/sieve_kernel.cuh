@@ -725,73 +725,127 @@ __device__ void exp_series(const S* __restrict__ q, int Q, S* __restrict__ e, in
   }
 }
 
-// Warp-cooperative Krylov data of the loop variants, on the reduced tile.
-// v_1 = e_1, v_{t+1} = H v_t (H the m x m block).  For t = 1..T:
-//   lam[t] = d * x.v_t  (x = tile row 0, cols 1..m),  mu[t] = d * y.v_t (tile row mb), mu0 likewise.
-// Column form, one lane per row: the "rows" of one step are x (virtual row 0), the Hessenberg
-// rows 1..min(t+1, m) and the extra rows y, y0, so the dot products are rows of the same sweep
-// over s (no warp reductions); v ping-pongs between two buffers.
+// Border data of the loop variants, without a Krylov sequence.  After the elimination the
+// border column is d e_1 (block index 1..m = tile index 1..m, nb = 1) and H is upper Hessenberg
+// with subdiagonal beta_i = H(i+1, i), so lam_t = d x.H^(t-1) e_1 (x = tile row 0; mu, mu0 the
+// same with the extra rows y = tile rows mb, mb+1) has the generating function
+//   sum_t lam_t z^t = d z x.(I - zH)^-1 e_1,
+// and Cramer's rule on the Hessenberg matrix I - zH gives its first column:
+//   [(I - zH)^-1]_{r,1} = z^(r-1) beta_1 .. beta_(r-1) Q_r(z) / P(z),
+// Q_r(z) = det(I - z H[r+1..m, r+1..m]) (the trailing principal submatrices; Q_m = 1), P = Q_0.
+// The anti-transpose H' = J H^T J is upper Hessenberg too and its leading submatrices are the
+// trailing ones of H reversed and transposed -- the same determinants -- so La Budde run on H'
+// yields P as usual and every Q_r as its row m - r.  Hence
+//   sum_t lam_t z^t = d sum_{r=1}^{min(m,T)} x_r beta_1 .. beta_(r-1) z^r Q_r(z) / P(z):
+// one sweep of T multiply-adds per series for the numerator and one for the division by P,
+// where the Krylov sequence v_(t+1) = H v_t took T(T+1)/2 warp-wide steps (a third of the
+// loop kinds' time at 40 photons).  (The reference forms the same quantities as matrix powers:
+// loop_hafnian_batch.py f_loop / f_loop_odd, _hafnian.py f_loop.)
+
+// Before La Budde (m >= 1): the weights w_r = x_r beta_1 .. beta_(r-1), r = 1..min(m, T), into
+// xs (and the extra rows' into ys, y0s), then the Hessenberg block anti-transposed in place.
+// The normalised forms have beta in {0, 1}: the weights stop at the first zero; double-float
+// takes the products by a prefix scan over the lanes.
 template <class S>
-__device__ void loop_krylov(const S* __restrict__ W, int ldw, int m, int mb, int ne, int T, S* __restrict__ v,
-                            S* __restrict__ vn, S* __restrict__ lam, S* __restrict__ mu, S* __restrict__ mu0) {
+__device__ void border_prepare(S* __restrict__ W, int ldw, int m, int mb, int ne, int T, S* __restrict__ xs,
+                               S* __restrict__ ys, S* __restrict__ y0s) {
   using A = Ar<S>;
   const int lane = threadIdx.x & 31;
-  const bool dnz = !A::is_zero(W[1 * ldw + 0]);
-  if (!dnz || m == 0) {
-    for (int t = lane; t <= T; t += 32) {
-      lam[t] = A::zero();
-      if (ne > 0) mu[t] = A::zero();
-      if (ne > 1) mu0[t] = A::zero();
+  const int R = T < m ? T : m;
+  S carry = A::one();  // double-float: product of the betas before this chunk
+  int cut = R + 1;      // normalised forms: first r whose weight is zero
+  for (int r0 = 1; r0 <= R; r0 += 32) {
+    const int r = r0 + lane;
+    // b = beta_(r-1) (r >= 2), the factor that joins at r
+    const S b = (r >= 2 && r <= R) ? W[r * ldw + r - 1] : A::one();
+    S w;
+    if constexpr (A::fp64) {
+      const unsigned z = __ballot_sync(0xffffffffu, r <= R && A::is_zero(b));
+      if (z && cut > R) cut = r0 + __ffs(z) - 1;
+      w = A::one();
+    } else {  // inclusive prefix product of b over the lanes, times the carry
+      w = b;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const S u = A::shfl(w, lane >= off ? lane - off : lane);
+        if (lane >= off) w = A::mul(u, w);
+      }
+      w = A::mul(carry, w);
+      carry = A::shfl(w, 31);
     }
-    __syncwarp();
-    return;
+    if (r <= R) {
+      const bool live = r < cut;
+      xs[r] = live ? A::mul(W[r], w) : A::zero();
+      if (ne > 0) ys[r] = live ? A::mul(W[mb * ldw + r], w) : A::zero();
+      if (ne > 1) y0s[r] = live ? A::mul(W[(mb + 1) * ldw + r], w) : A::zero();
+    }
   }
-  const S d = W[1 * ldw + 0];
-  for (int s = lane; s <= m; s += 32) v[s] = (s == 1) ? A::one() : A::zero();
   __syncwarp();
-  constexpr int SLOTS = 3;  // virtual rows lane, lane + 32, lane + 64 (m + 1 + ne <= 96)
-  for (int t = 1; t <= T; ++t) {
-    const int sup = t < m ? t : m;                            // support of v_t: 1..sup
-    const int nsup = t == T ? 0 : ((t + 1) < m ? (t + 1) : m);  // rows of v_{t+1} (none at the end)
-    const int nv = nsup + 1 + ne;                             // virtual rows: x, H rows, extra rows
-    int row[SLOTS], lo[SLOTS];
-    S acc[SLOTS];
-#pragma unroll
-    for (int k = 0; k < SLOTS; ++k) {
-      const int vr = lane + 32 * k;
-      acc[k] = A::zero();
-      if (vr == 0) { row[k] = 0; lo[k] = 1; }                        // x
-      else if (vr <= nsup) { row[k] = vr; lo[k] = vr > 1 ? vr - 1 : 1; }  // Hessenberg row
-      else if (vr < nv) { row[k] = mb + (vr - nsup - 1); lo[k] = 1; }  // y, y0
-      else { row[k] = -1; lo[k] = sup + 1; }
+  // anti-transpose of the block: (a, b) <-> (m+1-b, m+1-a) over the upper Hessenberg entries
+  // (b >= a-1, a set the map keeps), each pair swapped once from its member with a + b < m + 1
+  const int c = m + 1;
+  for (int a = 1; a + (a > 1 ? a - 1 : 1) < c; ++a) {
+    const int b0 = a > 1 ? a - 1 : 1;
+    for (int b = b0 + lane; a + b < c; b += 32) {
+      S& p = W[a * ldw + b];
+      S& q = W[(c - b) * ldw + (c - a)];
+      const S t = p;
+      p = q;
+      q = t;
     }
-    if (nv <= 32) {  // one virtual row per lane (t + ne < 31): a loop that issues one FMA per s
-      const S* wr = W + (row[0] >= 0 ? row[0] : 0) * ldw;
-      const int l0 = row[0] >= 0 ? lo[0] : sup + 1;
-      for (int s = 1; s <= sup; ++s) {
-        const S vs = v[s];
-        if (s >= l0) acc[0] = A::fma(wr[s], vs, acc[0]);
-      }
-    } else {
-      for (int s = 1; s <= sup; ++s) {
-        const S vs = v[s];
-#pragma unroll
-        for (int k = 0; k < SLOTS; ++k)
-          if (32 * k < nv && s >= lo[k] && row[k] >= 0) acc[k] = A::fma(W[row[k] * ldw + s], vs, acc[k]);
+  }
+  __syncwarp();
+}
+
+// After La Budde on the anti-transposed block: lam_t (mu_t, mu0_t), t = 1..T, from the weights
+// in lam (mu, mu0), the coefficient rows Q_r (La Budde's row m - r) and P = cpoly, overwriting
+// the weights; n0..n2 are scratch series (T + 1 entries).
+template <class S>
+__device__ void border_series(S* __restrict__ W, int ldw, int m, int Kc, S* __restrict__ win, int kw, bool tile,
+                              const S* __restrict__ cpoly, int T, int ne, S d, S* __restrict__ lam,
+                              S* __restrict__ mu, S* __restrict__ mu0, S* __restrict__ n0,
+                              S* __restrict__ n1, S* __restrict__ n2) {
+  using A = Ar<S>;
+  const int lane = threadIdx.x & 31;
+  const int R = T < m ? T : m;
+  // numerators: N_t = sum_{r <= min(t, R)} w_r Q_r[t - r]  (Q_r of degree min(m - r, Kc))
+  for (int t = 1 + lane; t - lane <= T; t += 32) {
+    S a0 = A::zero(), a1 = A::zero(), a2 = A::zero();
+    for (int r = 1; r <= R; ++r) {
+      const int i = m - r, k = t - r;
+      if (t <= T && k >= 0 && k <= (i < Kc ? i : Kc)) {
+        const S q = cw_at(W, ldw, 1, win, kw, tile, i, i % kw, k);
+        a0 = A::fma(lam[r], q, a0);
+        if (ne > 0) a1 = A::fma(mu[r], q, a1);
+        if (ne > 1) a2 = A::fma(mu0[r], q, a2);
       }
     }
-#pragma unroll
-    for (int k = 0; k < SLOTS; ++k) {
-      const int vr = lane + 32 * k;
-      if (vr == 0) lam[t] = A::mul(d, acc[k]);
-      else if (vr <= nsup) vn[vr] = acc[k];
-      else if (vr == nsup + 1 && ne > 0) mu[t] = A::mul(d, acc[k]);
-      else if (vr == nsup + 2 && ne > 1) mu0[t] = A::mul(d, acc[k]);
+    if (t <= T) {
+      n0[t] = a0;
+      if (ne > 0) n1[t] = a1;
+      if (ne > 1) n2[t] = a2;
+    }
+  }
+  __syncwarp();
+  // division by P (P_0 = 1, P_j = 0 above Kc), right-looking: once L_k is final every later
+  // L_t takes -P_(t-k) L_k
+  for (int k = 1; k < T; ++k) {
+    const S l0 = n0[k];
+    const S l1 = ne > 0 ? n1[k] : A::zero();
+    const S l2 = ne > 1 ? n2[k] : A::zero();
+    const int hi = (k + Kc) < T ? (k + Kc) : T;
+    for (int t = k + 1 + lane; t <= hi; t += 32) {
+      const S p = cpoly[t - k];
+      n0[t] = A::fnma(p, l0, n0[t]);
+      if (ne > 0) n1[t] = A::fnma(p, l1, n1[t]);
+      if (ne > 1) n2[t] = A::fnma(p, l2, n2[t]);
     }
     __syncwarp();
-    S* sw = v;
-    v = vn;
-    vn = sw;
+  }
+  for (int t = 1 + lane; t <= T; t += 32) {
+    lam[t] = A::mul(d, n0[t]);
+    if (ne > 0) mu[t] = A::mul(d, n1[t]);
+    if (ne > 1) mu0[t] = A::mul(d, n2[t]);
   }
   __syncwarp();
 }
@@ -964,12 +1018,26 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
       }
       __syncwarp();
       hessenberg_elim<S>(W, xv, mb, rows, ldw, nb);
-      // loop variants: Krylov data of the border first (La Budde then reuses the tile)
-      if (kind != KIND_PLAIN) loop_krylov<S>(W, ldw, m, mb, ne, I.K, xv, eser, lam, mu, mu0);
-      // characteristic polynomial coefficients of the block (xv is free again: it may hold tb)
+      // loop variants: the border's weights are read off the tile and the block anti-transposed,
+      // so that La Budde also yields the trailing submatrices' determinants (border_prepare)
       const int Kc = I.K < m ? I.K : m;
+      const S dbord = (kind != KIND_PLAIN && m > 0) ? W[1 * ldw + 0] : A::zero();
+      const bool border = kind != KIND_PLAIN && m > 0 && !A::is_zero(dbord);
+      if (border) border_prepare<S>(W, ldw, m, mb, ne, I.K, lam, mu, mu0);
+      // characteristic polynomial coefficients of the block (xv is free again: it may hold tb)
       labudde<S>(W, ldw, nb, m, Kc, win, L.kw, L.tilewin != 0, tb, lbpart, cpoly, P.lb_lane, P.lb_own,
                  P.lb_lane2, P.lb_own2);
+      if (border) {
+        border_series<S>(W, ldw, m, Kc, win, L.kw, L.tilewin != 0, cpoly, I.K, ne, dbord, lam, mu, mu0, eser,
+                         oser, qv);
+      } else if (kind != KIND_PLAIN) {
+        for (int t = lane; t <= I.K; t += 32) {
+          lam[t] = A::zero();
+          if (ne > 0) mu[t] = A::zero();
+          if (ne > 1) mu0[t] = A::zero();
+        }
+        __syncwarp();
+      }
       const int Gdeg = I.K;  // degree of det^(-1/2) needed
       inv_sqrt_series<S>(cpoly, Kc, gser, Gdeg);
 
