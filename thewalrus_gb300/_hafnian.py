@@ -326,8 +326,10 @@ def _finish(prep, precision):
 def hafnian_with_error(A, loop=False, rtol=1e-05, atol=1e-08, precision="fp64"):
     """(hafnian, error estimate, magnitude): the sieve result with the sum over its terms of
     |prefactor x term| (the magnitude the result cancels from) and the first-order estimate of
-    its rounding error, the term arithmetic's unit roundoff times that magnitude (the measured
-    errors of the FP64 sieve lie within 16x of it).  For a small matrix answered in closed form
+    its rounding error, the term arithmetic's unit roundoff times that magnitude (measured FP64
+    errors: within ~2x of it on the n = 40 benchmark matrices, within 6.3x on served Gaussian-state
+    loop hafnians whose cond exceeds 1e3, up to ~16x on loop hafnians with 66 photons on 4 modes,
+    whose terms' own 33-coefficient series cancel).  For a small matrix answered in closed form
     the estimate and magnitude are 0.  ``precision``: "fp64", "df" or "dd"."""
     input_validation(A, rtol=rtol, atol=atol)
     done, value = _closed_form(A, loop, rtol, atol)
