@@ -510,12 +510,14 @@ __device__ void labudde(S* __restrict__ W, int ldw, int nb, int m, int Kc, S* __
     } else {
       const S bi = i >= 2 ? W[wi * ldw + wi - 1] : A::zero();
       const S up0 = shfl_up_s(pr0, 1);  // P(i-1, r-1) for r = lane+1
-      const S up1 = shfl_up_s(pr1, 1);
-      const S last0 = A::shfl(pr0, 31);  // P(i-1, 32) feeds r = 33
       const S prev0 = lane == 0 ? A::one() : up0;
-      const S prev1 = lane == 0 ? last0 : up1;
+      if (Kc > 33) {  // the second block of products (r = lane+33 <= Kc-1) only when it is read
+        const S up1 = shfl_up_s(pr1, 1);
+        const S last0 = A::shfl(pr0, 31);  // P(i-1, 32) feeds r = 33
+        const S prev1 = lane == 0 ? last0 : up1;
+        pr1 = A::mul(bi, prev1);
+      }
       pr0 = A::mul(bi, prev0);
-      pr1 = A::mul(bi, prev1);
       if (lane + 1 <= R) tbr[lane + 1] = A::mul(W[(wi - lane - 1) * ldw + wi], pr0);
       if (lane + 33 <= R) tbr[lane + 33] = A::mul(W[(wi - lane - 33) * ldw + wi], pr1);
     }
