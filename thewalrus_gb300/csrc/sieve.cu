@@ -84,8 +84,8 @@ static int ensure_init(int device) {
   }
   CK(cudaDeviceGetAttribute(&T.sms, cudaDevAttrMultiProcessorCount, dev));
   // stream-ordered plans (one-shot calls, serving batches) allocate from this process's default
-  // pool of the device: keep up to 256 MiB of freed memory there instead of handing it back to
-  // the driver at every synchronisation, so a repeated call reuses it
+  // pool of the device: keep up to 256 MiB of freed memory there instead of releasing it to the
+  // CUDA driver at every synchronisation, so a repeated call reuses it
   cudaMemPool_t pool;
   CK(cudaDeviceGetDefaultMemPool(&pool, dev));
   unsigned long long keep = 256ull << 20;
