@@ -17,7 +17,9 @@ cpu_baseline : the CPU oracle (a C restatement of the reference algorithm: mixed
            bounded sample of the same hafnian's terms and scaled to hafnians/s.
 rel_err_vs_reference : the result against the value the reference's own code produced for the
            same input (committed fixture), and against the long-double oracle.
-batch, serve : (one GPU, default workload) the batched form on a stated subset of the
+loop, batch, serve : (one GPU, default workload) the 40-photon loop hafnian of a 20-mode
+           Gaussian state (FP64 rate, and the error of FP64, double-double and precision="auto"
+           against its _Float128 value: loop_summary), the batched form on a stated subset of the
            4,096-instance workload and the served form at two arrival rates, each against one
            call per instance and checked against the oracle (see batch_summary, serve_summary).
 --impl reference : that CPU restatement alone, as the reference arm (rank 0 only), on whole
@@ -308,6 +310,7 @@ def run_gpu(args, rank, world, local):
                                                              info["seconds"], info["threads"])}
     plan.close()
     if world == 1 and not args.no_extras and n == N_MATRIX and args.matrix == "complex":
+        line["loop"] = loop_summary("fp64", 20, 3, extra_precisions=("dd", "auto"))
         line["batch"] = batch_summary(args)
         line["serve"] = serve_summary(args)
     print(json.dumps(line), flush=True)
@@ -448,12 +451,15 @@ def _gpu_setup(local=0):
     return torch, nat
 
 
-def run_loop(args):
+def loop_summary(precision, steps, warmup, extra_precisions=()):
     """Loop hafnian of the 20-mode Gaussian-state reduced matrix (40 photons, repeats <= 3):
-    hafnian_repeated(A, rpt, mu=gamma, loop=True), device time per call and end to end."""
+    hafnian_repeated(A, rpt, mu=gamma, loop=True), device time per call and end to end, the error
+    against the committed _Float128 value, the sum's condition number, and (extra_precisions) the
+    error of one call in each further precision ("dd", "auto")."""
     import numpy as np
+    import torch
 
-    torch, nat = _gpu_setup()
+    from thewalrus_gb300 import _native as nat
     import thewalrus_gb300 as tw
     from thewalrus_gb300 import costmodel, workloads as wl
 
@@ -469,35 +475,47 @@ def run_loop(args):
     else:
         A, gamma, rpt = wl.gaussian_state_loop(modes=20, seed=1, photons=40, max_rep=3)
     inst = tw.prepare_loop_hafnian(A, gamma, list(rpt))
-    plan = nat.Plan([inst], precision=args.precision)
+    plan = nat.Plan([inst], precision=precision)
     s = torch.cuda.current_stream()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plan.execute(s.cuda_stream)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(s)
-    for _ in range(args.steps):
+    for _ in range(steps):
         plan.execute(s.cuda_stream)
     e1.record(s)
     torch.cuda.synchronize()
-    dev_s = e0.elapsed_time(e1) / 1e3 / args.steps
+    plan.close()
+    dev_s = e0.elapsed_time(e1) / 1e3 / steps
     t0 = time.perf_counter()
-    for _ in range(args.steps):
-        val = tw.hafnian_repeated(A, list(rpt), mu=gamma, loop=True, precision=args.precision)
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    for _ in range(steps):
+        val = tw.hafnian_repeated(A, list(rpt), mu=gamma, loop=True, precision=precision)
+    e2e_s = (time.perf_counter() - t0) / steps
     x, reps, odd = tw.matched_reps(list(rpt))
     flops = costmodel.instance_flops(reps, True, kind="loop", odd=odd is not None)
     line = {"metric": "loop hafnians/s (20-mode Gaussian state, 40 photons)", "value": 1 / dev_s,
             "unit": "hafnians/s", "ms_per_step": dev_s * 1e3, "e2e": {"value": 1 / e2e_s, "unit": "hafnians/s"},
             "edge_reps": [int(r) for r in reps], "terms": int(np.prod([r + 1 for r in reps]) // 1),
-            "achieved_tflops": flops / dev_s / 1e12, "precision": args.precision,
+            "achieved_tflops": flops / dev_s / 1e12, "precision": precision,
             "result": [float(val.real), float(val.imag)]}
     # accuracy against the committed _Float128 value, and the sum's condition number
     if truth is not None:
         line["rel_err_vs_float128"] = abs(complex(val) - truth) / abs(truth)
     vals, mags = tw.run_with_magnitudes([inst], "fp64")
     line["sum_abs_terms_over_abs_sum"] = float(mags[0] / abs(vals[0]))
-    print(json.dumps(line), flush=True)
+    for p in extra_precisions:
+        t0 = time.perf_counter()
+        v = complex(tw.hafnian_repeated(A, list(rpt), mu=gamma, loop=True, precision=p))
+        sec = time.perf_counter() - t0
+        line[p] = {"seconds": sec, "rel_err_vs_float128": abs(v - truth) / abs(truth) if truth is not None else None}
+    return line
+
+
+def run_loop(args):
+    """The loop hafnian line on its own (``--workload loop``)."""
+    _gpu_setup()
+    print(json.dumps(loop_summary(args.precision, args.steps, args.warmup)), flush=True)
 
 
 def run_batch(args):
