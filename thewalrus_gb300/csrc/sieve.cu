@@ -378,8 +378,8 @@ static int prepare(const wg_instance& in, int precision, Prepared& P) {
   P.rows_max = m_max + nb + ne;
   P.kc_max = std::min(d.K, m_max);
   // plain kinds keep det coefficients and the series (K + 1 each); loop kinds also the odd
-  // series (Nodd, Nf) and the Krylov vectors (m + 1)
-  P.nser_need = kind == KIND_PLAIN ? d.K + 2 : std::max(std::max(d.K, d.Nodd), std::max(Nf, m_max)) + 2;
+  // series (Nodd, Nf) and the border series and their weights (K + 1 each)
+  P.nser_need = kind == KIND_PLAIN ? d.K + 2 : std::max(std::max(d.K, d.Nodd), Nf) + 2;
   P.narr = (kind == KIND_PLAIN) ? 2 : 8;
   {
     // a term with m < K+1 and no border/extra rows has columns shorter than Kc+1: only when
@@ -557,7 +557,7 @@ static int prepare_request(const wg_request& r, const wg_state& st, int precisio
   P.mb_max = P.m_max + 1;
   P.rows_max = P.m_max + 1 + d.ne;
   P.kc_max = std::min(d.K, P.m_max);
-  P.nser_need = std::max(std::max(d.K, d.Nodd), P.m_max) + 2;
+  P.nser_need = std::max(d.K, d.Nodd) + 2;
   P.narr = 8;
   P.tile_ok = true;  // bordered tile
   P.term_cost = (double)P.mb_max * P.mb_max * P.mb_max + 64.0;

@@ -5,13 +5,15 @@
 // each term it
 //   1. gathers the term matrix AX_S (rows/cols of nonzero delta, columns scaled by delta, halves
 //      swapped) into the warp's shared-memory tile; loop variants border it with D_S / XD_S and
-//      append the odd-mode rows, so that the Krylov data of the loop terms survive the reduction;
+//      append the odd-mode rows, so that the border data of the loop terms survive the reduction;
 //   2. reduces it to upper Hessenberg form by Gaussian elimination with partial pivoting (FP64
 //      and residues: every subdiagonal entry normalised to exactly 1 or 0 by a diagonal
 //      similarity, so that La Budde's recurrence needs no subdiagonal products; double-float:
 //      classic multipliers), treating columns whose candidates are rounding residues as reduced;
 //   3. runs La Budde's recurrence for the first K coefficients of det(I - eta H), two rows per
-//      balanced pass;
+//      balanced pass (loop variants: on the anti-transposed block, whose intermediate rows are
+//      the trailing submatrices' determinants that give the border series, border_prepare /
+//      border_series);
 //   4. forms the term's generating function: det(I - eta H)^(-1/2) (the power-trace
 //      exponential of f / f_loop), times exp of the loop terms for the loop variants;
 //   5. adds prefactor * coefficient into lane-resident Neumaier sums (residue sums for the exact
