@@ -75,3 +75,30 @@ def test_block_diagonal_terms(reps):
     cond = _cond(A, D, reps)
     assert rel(tw.hafnian_repeated(A, reps, mu=D, loop=True, precision="dd"), want) < 1e-12
     assert rel(tw.hafnian_repeated(A, reps, mu=D, loop=True, precision="fp64"), want) < max(32 * EPS * cond, 1e-13)
+
+
+def test_window_storage_in_a_mixed_plan():
+    """A plain instance with an even repetition has terms with fewer than K + 1 rows, so a launch
+    group holding it keeps La Budde's coefficient rows in the circular window instead of dead
+    tile columns; the loop instances merged into that group read their trailing determinants
+    from the window.  Every output equals the instance evaluated alone (tile storage)."""
+    from thewalrus_gb300 import _native as nat
+    from thewalrus_gb300 import workloads as wl
+
+    A = wl.complex_symmetric(10, seed=5)
+    plain = tw.prepare_hafnian(A, reps=[2, 1, 1, 2, 0, 1, 1, 0, 2, 0])
+    B, D = _inputs(2, n=6)
+    loops = [tw.prepare_loop_hafnian(B, D, [3, 2, 2, 1, 2, 2]), tw.prepare_loop_hafnian(B, D, [3, 2, 2, 1, 2, 1]),
+             tw.prepare_loop_hafnian(B, D, [17, 17, 16, 16, 0, 0])]
+    insts = [plain] + loops
+    alone = [complex(nat.run([i])[0]) for i in insts]
+    plan = nat.Plan(insts, merge_classes=True)
+    try:
+        plan.execute()
+        mixed = plan.read()
+    finally:
+        plan.close()
+    for a, b in zip(alone, mixed):
+        assert rel(b, a) < 1e-13, (a, b)
+    want = complex(oracle.hafnian_repeated(B, [17, 17, 16, 16, 0, 0], mu=D, loop=True, precision="quad"))
+    assert rel(mixed[3], want) < 32 * EPS * _cond(B, D, [17, 17, 16, 16, 0, 0])
