@@ -458,17 +458,19 @@ def hafnian_repeated(A, rpt, mu=None, loop=False, rtol=1e-05, atol=1e-08, glynn=
 def _batch_edges_even(fixed_edges):
     if len(fixed_edges) == 0:
         return np.array([0, 0], dtype=int)
-    half = fixed_edges.shape[0] // 2
-    new = int(max(fixed_edges)) + 1
-    return np.concatenate([[new], fixed_edges[:half], [new], fixed_edges[half:]]).astype(int)
+    fe = [int(v) for v in fixed_edges]
+    half = len(fe) // 2
+    new = max(fe) + 1
+    return np.array([new] + fe[:half] + [new] + fe[half:], dtype=int)
 
 
 def _batch_edges_odd(fixed_edges, oddmode):
     if len(fixed_edges) == 0:
         return np.array([1, oddmode, 1, 1], dtype=int)
-    half = fixed_edges.shape[0] // 2
-    new = int(max(max(fixed_edges), oddmode)) + 1
-    return np.concatenate([[new, oddmode], fixed_edges[:half], [new, new], fixed_edges[half:]]).astype(int)
+    fe = [int(v) for v in fixed_edges]
+    half = len(fe) // 2
+    new = max(max(fe), int(oddmode)) + 1
+    return np.array([new, oddmode] + fe[:half] + [new, new] + fe[half:], dtype=int)
 
 
 def prepare_loop_hafnian_batch(A, D, fixed_reps, N_cutoff, glynn=True):

@@ -197,9 +197,7 @@ class Instance:
     def __init__(self, kind, A, edge_reps, glynn=True, D=None, oddV=None, oddloop=None,
                  batch_max=0, cutoff=0):
         A = np.asarray(A)
-        cplx = np.iscomplexobj(A) or (D is not None and np.iscomplexobj(D)) or \
-            (oddV is not None and np.iscomplexobj(oddV)) or \
-            (oddloop is not None and np.iscomplexobj(oddloop))
+        cplx = any(x is not None and np.asarray(x).dtype.kind == "c" for x in (A, D, oddV, oddloop))
         dt = np.complex128 if cplx else np.float64
         self.A = np.ascontiguousarray(A, dtype=dt)
         self.reps = np.ascontiguousarray(np.asarray(edge_reps, dtype=np.int64).reshape(-1))
