@@ -443,7 +443,10 @@ def run(instances, precision="fp64", stream=0):
 
 def check_arith(op, x, x_lo=None, y=None, y_lo=None):
     """Evaluate one of the kernels' arithmetic primitives on the device elementwise
-    (``wg_check_arith``); returns the (hi, lo) arrays."""
+    (``wg_check_arith``): op 0 the FP64 pivot reciprocal, 1-3 the double-double reciprocal,
+    division by the integer y and product, 4-6 the double-float reciprocal, complex reciprocal
+    (returns the real and imaginary parts) and division by the integer y.  Returns the (hi, lo)
+    arrays."""
     x = np.asarray(x, dtype=np.float64).ravel()
     z = np.zeros_like(x)
     inp = np.ascontiguousarray(np.stack([x, z if x_lo is None else np.asarray(x_lo, dtype=np.float64).ravel(),
