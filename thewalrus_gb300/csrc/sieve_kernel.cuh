@@ -903,12 +903,12 @@ static __global__ void __launch_bounds__(256) sieve_kernel(const SieveParams P) 
   const int ns = L.nser;
   S* cpoly = ser;           // [0, ns)
   S* gser = ser + ns;       // [ns, 2ns)
-  S* eser = ser + 2 * ns;   // even exp series / Krylov scratch
-  S* oser = ser + 3 * ns;   // odd exp series
-  S* lam = ser + 4 * ns;
+  S* eser = ser + 2 * ns;   // even exp series (before it: a border-series numerator)
+  S* oser = ser + 3 * ns;   // odd exp series (before it: a border-series numerator)
+  S* lam = ser + 4 * ns;    // border series of x (before it: its weights); likewise mu, mu0
   S* mu = ser + 5 * ns;
   S* mu0 = ser + 6 * ns;
-  S* qv = ser + 7 * ns;     // series exponents
+  S* qv = ser + 7 * ns;     // series exponents (before them: a border-series numerator)
 
   for (;;) {
     int c = 0;
