@@ -18,6 +18,8 @@ that cancel beyond FP64's reach), "auto" (FP64, and double-double again for the 
 term magnitudes say FP64 may miss 1e-10) or "exact" (integer inputs).  Sieve results come back as
 ``numpy.complex128`` also for real input, as in the reference.
 """
+import heapq
+
 import numpy as np
 
 from . import _native as nat
@@ -122,25 +124,28 @@ def matched_reps(reps):
     reps = [int(r) for r in reps]
     if sum(reps) == 0:
         return np.array([], dtype=int), np.array([], dtype=int), None
-    # (count, index) pairs, kept in descending order; ties broken by the larger index first
-    pool = sorted(((r, i) for i, r in enumerate(reps) if r > 0), reverse=True)
+    # a heap of (-count, -index): the largest count first, ties broken by the larger index first
+    pool = [(-r, -i) for i, r in enumerate(reps) if r > 0]
+    heapq.heapify(pool)
     left, right, mult = [], [], []
-    while len(pool) > 1 or (pool and pool[0][0] > 1):
-        pool.sort(reverse=True)
-        top_r, top_i = pool[0]
-        if len(pool) == 1 or top_r > 2 * pool[1][0]:
+    while len(pool) > 1 or (pool and -pool[0][0] > 1):
+        top_r, top_i = heapq.heappop(pool)
+        top_r, top_i = -top_r, -top_i
+        if not pool or top_r > 2 * -pool[0][0]:
             left.append(top_i)
             right.append(top_i)
             mult.append(top_r // 2)
-            pool = pool[1:] if top_r % 2 == 0 else [(1, top_i)] + pool[1:]
+            if top_r % 2:
+                heapq.heappush(pool, (-1, -top_i))
         else:
-            sec_r, sec_i = pool[1]
+            sec_r, sec_i = heapq.heappop(pool)
+            sec_r, sec_i = -sec_r, -sec_i
             left.append(top_i)
             right.append(sec_i)
             mult.append(sec_r)
-            rest = pool[2:]
-            pool = [(top_r - sec_r, top_i)] + rest if top_r > sec_r else rest
-    oddmode = pool[0][1] if len(pool) == 1 else None
+            if top_r > sec_r:
+                heapq.heappush(pool, (-(top_r - sec_r), -top_i))
+    oddmode = -pool[0][1] if len(pool) == 1 else None
     return np.asarray(left + right, dtype=np.int64), np.asarray(mult, dtype=np.int64), oddmode
 
 
