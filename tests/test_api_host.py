@@ -99,3 +99,46 @@ def test_special_cases_answered_on_the_host():
     assert tw.loop_hafnian(A, D=np.ones(2), reps=[0, 0]) == 1.0
     x, y, z = tw.matched_reps([0, 0, 0, 0])
     assert x.shape == (0,) and y.shape == (0,) and z is None
+
+
+def test_prepared_instances_match_a_direct_construction():
+    """The host preparation (edge pairing, row/column selection, the real/complex choice, the
+    batch edges) against the same construction written out with numpy's generic indexing, for
+    ordinary inputs (which pair balancing leaves untouched)."""
+    from thewalrus_gb300 import _native as nat
+    from thewalrus_gb300 import workloads as wl
+
+    def typed(x, cplx):
+        x = np.asarray(x)
+        return x.astype(np.complex128) if cplx else x.real.astype(np.float64)
+
+    rng = np.random.default_rng(21)
+    for trial in range(40):
+        n = int(rng.integers(2, 9))
+        A = wl.complex_symmetric(n, seed=trial) if trial % 2 else wl.real_signed(n, seed=trial)
+        D = rng.normal(size=n) + (1j * rng.normal(size=n) if trial % 2 else 0)
+        reps = [int(r) for r in rng.integers(0, 3, size=n)]
+        if sum(reps) == 0:
+            reps[0] = 2
+        x, er, odd = tw.matched_reps(reps)
+        cplx = bool(trial % 2)  # complex_symmetric and the complex D have nonzero imaginary parts
+        if sum(reps) % 2 == 0:
+            inst = tw.prepare_hafnian(A, reps)
+            assert inst.A.dtype == (np.complex128 if cplx else np.float64)
+            assert np.array_equal(inst.A, typed(A[np.ix_(x, x)], cplx))
+            assert np.array_equal(inst.reps, er)
+        inst = tw.prepare_loop_hafnian(A, D, reps)
+        if isinstance(inst, nat.Instance):
+            assert np.array_equal(inst.A, typed(A[np.ix_(x, x)], cplx))
+            assert np.array_equal(inst.D, typed(np.asarray(D)[x], cplx))
+            if odd is not None:
+                assert np.array_equal(inst.oddV, typed(A[odd, x], cplx))
+        # loop_hafnian_batch: the fixed modes' pairing, bordered by the batch edge(s)
+        fixed = reps[:-1]
+        bi = tw.prepare_loop_hafnian_batch(A, D, fixed, 4)
+        nz = np.nonzero(fixed + [1])[0]
+        fe, fm, fodd = tw.matched_reps(np.asarray(fixed)[nz[:-1]])
+        edges = H._batch_edges_even(fe) if fodd is None else H._batch_edges_odd(fe, fodd)
+        assert np.array_equal(bi.A, typed(A[np.ix_(nz, nz)][np.ix_(edges, edges)], cplx))
+        assert np.array_equal(bi.D, typed(np.asarray(D)[nz][edges], cplx))
+        assert np.array_equal(bi.reps, fm)
