@@ -202,7 +202,7 @@ int wg_measure_fp_peaks(double* fp64_tflops, double* fp32_tflops);
 
 /* The kernels' own arithmetic primitives evaluated elementwise on the device, for checks against
  * IEEE and exact references (no counterpart in the reference): op 0 the pivot reciprocal 1/x
- * (approximate reciprocal + two Newton steps), 1 the double-double reciprocal of (x, x_lo), 2 the
+ * (approximate reciprocal + one third-order step r(1 + e + e^2)), 1 the double-double reciprocal of (x, x_lo), 2 the
  * double-double quotient (x, x_lo) / k with k = (int)y, 3 the double-double product of (x, x_lo)
  * and (y, y_lo), 4 the double-float reciprocal of (x, x_lo), 5 the complex double-float
  * reciprocal of (x, x_lo) + i (y, y_lo) (out: its real and imaginary parts, each hi + lo in FP64),

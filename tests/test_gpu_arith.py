@@ -1,9 +1,10 @@
 """The kernels' own arithmetic primitives on the GPU (``wg_check_arith``) against IEEE and exact
 references.
 
-* The pivot reciprocal (``recip_newton``: the PTX approximate reciprocal refined by two Newton
-  steps, IEEE division outside the approximation's safe exponent range) against numpy's correctly
-  rounded 1/x: within 1 ulp everywhere, over magnitudes 2^-1000 .. 2^1000 and both signs.
+* The pivot reciprocal (``recip_newton``: the PTX approximate reciprocal refined by one
+  third-order step r(1 + e + e^2), IEEE division outside the approximation's safe exponent range)
+  against numpy's correctly rounded 1/x: within 1 ulp everywhere, over magnitudes 2^-1000 ..
+  2^1000 and both signs.
 * The double-double primitives (reciprocal, division by a small integer, product) against exact
   rational arithmetic: relative error below 2^-100 (a double-double carries 106 bits; the
   primitives give up a few bits to their final renormalisation).
