@@ -289,9 +289,9 @@ def prepare_loop_hafnian(A, D=None, reps=None, glynn=True):
 # significand) and the rule of precision="auto": FP64 first; when AUTO_FACTOR x 2^-53 x
 # sum|term| exceeds AUTO_RTOL x |result| the instance runs again in double-double.  The factor
 # covers the Hessenberg route's per-term rounding: on the n = 40 benchmark matrices
-# (sum|term| / |sum| = 6.8e4 complex, 2.0e5 real) FP64 ends 4.6e-12 and 4.6e-11 from the
-# reference's values (0.6 and 2.1 x 2^-53 x cond), on the 40-photon loop hafnian of a 20-mode
-# state (3.4e10) 2.3e-6 (0.5x); the first stays FP64, the other two go to double-double.  Over
+# (sum|term| / |sum| = 6.8e4 complex, 2.0e5 real) FP64 ends 4.4e-12 and 4.1e-11 from the
+# reference's values (0.6 and 1.8 x 2^-53 x cond), on the 40-photon loop hafnian of a 20-mode
+# state (3.4e10) 2.2e-6 (0.6x); the first stays FP64, the other two go to double-double.  Over
 # 300 loop hafnians of 64-mode Gaussian states with 8-28 photons the error in units of
 # 2^-53 x cond is at most 6.3 where cond >= 1e3; larger ratios (up to 85, rounding inside
 # single terms) occur only below cond = 100, where the error is below 2e-13.
